@@ -1,0 +1,94 @@
+"""ctypes binding of libappfis_gb.so (the C ABI declared in include/appfis_gb.h).
+
+The library must have been built (appfis_gb300.build.build() or __graft_entry__.build());
+there is no fallback: loading fails loudly when it is missing.
+"""
+import ctypes
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libappfis_gb.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "appfis_gb.h")
+
+OK, EINVAL, ECUDA, ENOMEM, ETIMEOUT = 0, 1, 2, 3, 4
+F32, F64, I32 = 0, 1, 2
+MAX, MIN, SUM = 0, 1, 2
+LIFE_REFERENCE, LIFE_B3S23 = 0, 1
+FORM_U8, FORM_BITS = 0, 1
+
+_P = ctypes.c_void_p
+_i = ctypes.c_int
+_i64 = ctypes.c_int64
+_f = ctypes.c_float
+_d = ctypes.c_double
+
+# name -> argtypes (restype is int unless listed in _RESTYPES)
+SIGNATURES = {
+    "appfis_gb_last_error": [],
+    "appfis_gb_version": [],
+    "appfis_gb_stream_sync": [_P],
+    "appfis_gb_reduce": [_P, _i, _i, _i, _P, _i, _P, _P],
+    "appfis_gb_reduce_host": [_P, _i, _i, _i, _P, _i, _P, _P],
+    "appfis_gb_life_u8": [_P, _P, _i, _i, _i, _i, _P, _P],
+    "appfis_gb_life_pack": [_P, _P, _i, _i, _P],
+    "appfis_gb_life_unpack": [_P, _P, _i, _i, _P],
+    "appfis_gb_life_bits": [_P, _P, _i, _i, _i, _i, _P, _P],
+    "appfis_gb_life_population_u8": [_P, _i64, _P, _P],
+    "appfis_gb_life_population_bits": [_P, _i64, _P, _P],
+    "appfis_gb_life_job": [_P, _P, _i, _i, _i, _i, _i, _P],
+    "appfis_gb_heat2d": [_P, _P, _i, _i, _i, _i, _f, _f, _P, _P],
+    "appfis_gb_heat2d_sweep": [_P, _P, _i, _i, _i, _f, _f, _P],
+    "appfis_gb_heat2d_job": [_P, _i, _i, _i, _f, _f, _P],
+}
+_RESTYPES = {"appfis_gb_last_error": ctypes.c_char_p}
+
+
+class AppfisError(RuntimeError):
+    def __init__(self, name, status, message):
+        super().__init__("%s failed with status %d: %s" % (name, status, message))
+        self.status = status
+
+
+_lib = None
+
+
+def declared_symbols():
+    """Every function name declared in include/appfis_gb.h."""
+    with open(HEADER) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"APPFIS_GB_API\s+(?:const\s+char\s*\*|int)\s+(appfis_gb_\w+)\s*\(", text)))
+
+
+def lib():
+    """The loaded library with argtypes set; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libappfis_gb.so is not built (run appfis_gb300.build.build() or __graft_entry__.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = _RESTYPES.get(name, ctypes.c_int)
+        _lib = L
+    return _lib
+
+
+def call(name, *args):
+    """Call an entry point; raise AppfisError with the library's message on a non-zero status."""
+    st = getattr(lib(), name)(*args)
+    if st != OK:
+        raise AppfisError(name, st, lib().appfis_gb_last_error().decode(errors="replace"))
+    return st
+
+
+def ptr(x):
+    """Device/host address of a torch tensor or numpy array (or an int / None)."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    return x.ctypes.data

@@ -1,0 +1,47 @@
+// Shared plumbing of the C-ABI library: status codes, the last-error message, argument checks,
+// CUDA error capture and a grow-only per-device workspace.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "appfis_gb.h"
+
+namespace gb {
+
+// Records msg as this thread's last error and returns `code`.
+int fail(int code, const char* fmt, ...);
+// Returns OK, or records the CUDA error of `e` (with `what`) and returns APPFIS_GB_ECUDA.
+int cuda_status(cudaError_t e, const char* what);
+// Checks the launch that just happened on this thread.
+inline int launched(const char* what) { return cuda_status(cudaGetLastError(), what); }
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Device workspace: one grow-only allocation per (device, slot), reused across calls.  Calls
+// that use the same slot on the same device must not overlap on the GPU.
+enum Slot { WS_REDUCE = 0, WS_JOB_A, WS_JOB_B, WS_JOB_C, WS_JOB_D, WS_JOB_E, WS_JOB_F, WS_SLOTS };
+int workspace(int slot, size_t bytes, void** out);
+// Pinned host staging buffer, grow-only, per slot (0..1).
+int pinned(int slot, size_t bytes, void** out);
+
+inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+// Number of SMs of the current device (cached).
+int sm_count();
+
+#define GB_TRY(expr)                 \
+    do {                             \
+        int _st = (expr);            \
+        if (_st != APPFIS_GB_OK)     \
+            return _st;              \
+    } while (0)
+
+#define GB_CUDA(expr) GB_TRY(::gb::cuda_status((expr), #expr))
+
+}  // namespace gb

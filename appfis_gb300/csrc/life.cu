@@ -1,0 +1,427 @@
+// GameOfLife on a periodic grid: byte-per-cell (SWAR, 16 cells per thread per row) and
+// bit-packed (32 cells per word) sweeps, pack/unpack, population count, whole-run job.
+//
+// Reference semantics (GameOfLife/src/game_appfis.hpp:121-135): a live cell whose 8-neighbour
+// count is < 2 or > 4 is cleared in `next`; a dead cell with count 3 is set in `next`; any
+// other cell leaves `next` untouched, so `next` keeps the state of two generations back (the
+// DUAL grid's buffers swap every generation, Appfis/Runtime.hpp:318-319).  In bit-slice form:
+//     new = (cur & keep & old) | (~cur & (birth | old)),  keep = (cnt in 2..4), birth = (cnt == 3).
+// The periodic halo refresh of the reference (pack, MPI self-exchange, unpack every
+// generation, Appfis/Communication.hpp:612-678) becomes index wrap-around inside the sweep.
+//
+// Layout: interior cells only, x fastest, row pitch nx bytes (u8) or nx/32 words (bits).
+// Both sweeps march down a strip of rows per warp, keeping the row above / at / below in
+// registers (each row is loaded once per warp task) and exchanging the words at lane
+// boundaries with warp shuffles; only the two end lanes load one extra word per row.
+#include "gb_common.cuh"
+
+namespace {
+
+constexpr uint32_t FULL = 0xffffffffu;
+constexpr uint32_t LSB = 0x01010101u;  // bit 0 of each byte
+constexpr int LIFE_ROWS = 64;           // rows per warp task
+
+// ------------------------------------------------------------------------------ rule logic
+// Per byte lane (u8 form): cnt in 0..8 in each byte, c/o in {0,1} per byte.
+template <int RULE>
+__device__ __forceinline__ uint32_t rule_bytes(uint32_t cnt, uint32_t c, uint32_t o)
+{
+    uint32_t b0 = cnt & LSB, b1 = (cnt >> 1) & LSB, b2 = (cnt >> 2) & LSB, b3 = (cnt >> 3) & LSB;
+    if (RULE == APPFIS_GB_LIFE_REFERENCE) {
+        uint32_t birth = b0 & b1 & ~(b2 | b3);
+        uint32_t keep = ~b3 & ((~b2 & b1) | (b2 & ~b1 & ~b0));
+        return ((c & keep & o) | (~c & (birth | o))) & LSB;
+    } else {
+        return (b1 & ~(b2 | b3) & (b0 | c)) & LSB;
+    }
+}
+
+// Per bit lane (bits form): cnt as bit slices r0..r3.
+template <int RULE>
+__device__ __forceinline__ uint32_t rule_bits(uint32_t r0, uint32_t r1, uint32_t r2, uint32_t r3, uint32_t c, uint32_t o)
+{
+    if (RULE == APPFIS_GB_LIFE_REFERENCE) {
+        uint32_t birth = r0 & r1 & ~(r2 | r3);
+        uint32_t keep = ~r3 & ((~r2 & r1) | (r2 & ~r1 & ~r0));
+        return (c & keep & o) | (~c & (birth | o));
+    } else {
+        return r1 & ~(r2 | r3) & (r0 | c);
+    }
+}
+
+// ------------------------------------------------------------------------------ generic form
+// One thread per cell, any nx, ny (used when nx is not a multiple of 16).
+template <int RULE>
+__global__ void life_u8_generic(const uint8_t* __restrict__ cur, uint8_t* __restrict__ out, int nx, int ny)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= nx || j >= ny) return;
+    int im = i == 0 ? nx - 1 : i - 1, ip = i == nx - 1 ? 0 : i + 1;
+    size_t rm = (size_t)(j == 0 ? ny - 1 : j - 1) * nx, r0 = (size_t)j * nx, rp = (size_t)(j == ny - 1 ? 0 : j + 1) * nx;
+    uint32_t cnt = cur[rm + im] + cur[rm + i] + cur[rm + ip] + cur[r0 + im] + cur[r0 + ip] + cur[rp + im] + cur[rp + i] +
+                   cur[rp + ip];
+    uint32_t c = cur[r0 + i];
+    uint32_t o = out[r0 + i];
+    out[r0 + i] = (uint8_t)rule_bytes<RULE>(cnt, c, RULE == APPFIS_GB_LIFE_REFERENCE ? o : 0u);
+}
+
+// ------------------------------------------------------------------------------ u8 SWAR form
+struct RowU8 {
+    uint32_t w[4];   // the 16 cells of this lane
+    uint32_t s3[4];  // per byte: left + self + right
+};
+
+__device__ __forceinline__ void load_row_u8(const uint8_t* __restrict__ cur, int nx, int row, int x0, bool active,
+                                            int lane, RowU8& r)
+{
+    const uint8_t* p = cur + (size_t)row * nx;
+    uint4 v = active ? __ldg(reinterpret_cast<const uint4*>(p + x0)) : make_uint4(0, 0, 0, 0);
+    uint32_t lw = __shfl_up_sync(FULL, v.w, 1);
+    uint32_t rw = __shfl_down_sync(FULL, v.x, 1);
+    if (lane == 0) lw = (uint32_t)__ldg(p + (x0 == 0 ? nx - 1 : x0 - 1)) << 24;
+    if (active && (lane == 31 || x0 + 16 >= nx)) rw = __ldg(p + (x0 + 16 >= nx ? 0 : x0 + 16));
+    r.w[0] = v.x;
+    r.w[1] = v.y;
+    r.w[2] = v.z;
+    r.w[3] = v.w;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        uint32_t prev = k == 0 ? lw : r.w[k - 1];
+        uint32_t next = k == 3 ? rw : r.w[k + 1];
+        uint32_t L = (r.w[k] << 8) | (prev >> 24);
+        uint32_t R = (r.w[k] >> 8) | (next << 24);
+        r.s3[k] = L + r.w[k] + R;
+    }
+}
+
+// Each warp task: a 512-byte strip (32 lanes x 16 cells) over LIFE_ROWS rows.
+template <int RULE>
+__global__ void __launch_bounds__(256) life_u8_swar(const uint8_t* __restrict__ cur, uint8_t* __restrict__ out,
+                                                     int nx, int ny, int strips, int tasks)
+{
+    const int lane = threadIdx.x & 31;
+    const int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (task >= tasks) return;  // warp-uniform
+    const int strip = task % strips, seg = task / strips;
+    const int x0 = strip * 512 + lane * 16;
+    const bool active = x0 < nx;
+    const int j0 = seg * LIFE_ROWS, j1 = min(j0 + LIFE_ROWS, ny);
+
+    RowU8 up, mid, dn;
+    load_row_u8(cur, nx, j0 == 0 ? ny - 1 : j0 - 1, x0, active, lane, up);
+    load_row_u8(cur, nx, j0, x0, active, lane, mid);
+    for (int j = j0; j < j1; j++) {
+        load_row_u8(cur, nx, j == ny - 1 ? 0 : j + 1, x0, active, lane, dn);
+        uint8_t* po = out + (size_t)j * nx + x0;
+        if (active) {
+            uint4 o = make_uint4(0, 0, 0, 0);
+            if (RULE == APPFIS_GB_LIFE_REFERENCE) o = *reinterpret_cast<const uint4*>(po);
+            uint32_t ow[4] = {o.x, o.y, o.z, o.w}, nw[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                uint32_t cnt = up.s3[k] + (mid.s3[k] - mid.w[k]) + dn.s3[k];
+                nw[k] = rule_bytes<RULE>(cnt, mid.w[k], ow[k]);
+            }
+            *reinterpret_cast<uint4*>(po) = make_uint4(nw[0], nw[1], nw[2], nw[3]);
+        }
+        up = mid;
+        mid = dn;
+    }
+}
+
+// ------------------------------------------------------------------------------ bit-packed form
+struct RowBits {
+    uint32_t w;       // 32 cells
+    uint32_t a0, a1;  // left + self + right as 2-bit slices
+    uint32_t h0, h1;  // left + right as 2-bit slices
+};
+
+__device__ __forceinline__ void load_row_bits(const uint32_t* __restrict__ bits, int nw, int row, int xw, bool active,
+                                              int lane, RowBits& r)
+{
+    const uint32_t* p = bits + (size_t)row * nw;
+    uint32_t w = active ? __ldg(p + xw) : 0u;
+    uint32_t lw = __shfl_up_sync(FULL, w, 1);
+    uint32_t rw = __shfl_down_sync(FULL, w, 1);
+    if (lane == 0) lw = __ldg(p + (xw == 0 ? nw - 1 : xw - 1));
+    if (active && (lane == 31 || xw + 1 >= nw)) rw = __ldg(p + (xw + 1 >= nw ? 0 : xw + 1));
+    uint32_t L = (w << 1) | (lw >> 31);  // bit b = cell x-1
+    uint32_t R = (w >> 1) | (rw << 31);  // bit b = cell x+1
+    r.w = w;
+    r.a0 = L ^ w ^ R;
+    r.a1 = (L & w) | (R & (L ^ w));
+    r.h0 = L ^ R;
+    r.h1 = L & R;
+}
+
+// Each warp task: 32 words (1024 cells) per row over LIFE_ROWS rows.
+template <int RULE>
+__global__ void __launch_bounds__(256) life_bits_sweep(const uint32_t* __restrict__ cur, uint32_t* __restrict__ out,
+                                                        int nw, int ny, int strips, int tasks)
+{
+    const int lane = threadIdx.x & 31;
+    const int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (task >= tasks) return;
+    const int strip = task % strips, seg = task / strips;
+    const int xw = strip * 32 + lane;
+    const bool active = xw < nw;
+    const int j0 = seg * LIFE_ROWS, j1 = min(j0 + LIFE_ROWS, ny);
+
+    RowBits up, mid, dn;
+    load_row_bits(cur, nw, j0 == 0 ? ny - 1 : j0 - 1, xw, active, lane, up);
+    load_row_bits(cur, nw, j0, xw, active, lane, mid);
+    for (int j = j0; j < j1; j++) {
+        load_row_bits(cur, nw, j == ny - 1 ? 0 : j + 1, xw, active, lane, dn);
+        if (active) {
+            uint32_t* po = out + (size_t)j * nw + xw;
+            uint32_t o = RULE == APPFIS_GB_LIFE_REFERENCE ? *po : 0u;
+            // count = up(3-input) + mid(2-input) + dn(3-input), bit-sliced
+            uint32_t t0 = up.a0 ^ mid.h0, c0 = up.a0 & mid.h0;
+            uint32_t t1 = up.a1 ^ mid.h1 ^ c0, t2 = (up.a1 & mid.h1) | (c0 & (up.a1 ^ mid.h1));
+            uint32_t r0 = t0 ^ dn.a0, k0 = t0 & dn.a0;
+            uint32_t r1 = t1 ^ dn.a1 ^ k0, k1 = (t1 & dn.a1) | (k0 & (t1 ^ dn.a1));
+            uint32_t r2 = t2 ^ k1, r3 = t2 & k1;
+            *po = rule_bits<RULE>(r0, r1, r2, r3, mid.w, o);
+        }
+        up = mid;
+        mid = dn;
+    }
+}
+
+__global__ void life_pack(const uint8_t* __restrict__ cells, uint32_t* __restrict__ bits, size_t nwords)
+{
+    size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwords) return;
+    const uint4* p = reinterpret_cast<const uint4*>(cells + w * 32);
+    uint4 a = __ldg(p), b = __ldg(p + 1);
+    uint32_t v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w}, out = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        uint32_t x = v[k] & LSB;                 // bit 0 of bytes 0..3 -> bits 0, 8, 16, 24
+        x = (x | (x >> 7)) & 0x00030003u;        // bytes 0,1 -> bits 0,1 ; bytes 2,3 -> bits 16,17
+        x = (x | (x >> 14)) & 0x0000000fu;       // -> bits 0..3
+        out |= x << (4 * k);
+    }
+    bits[w] = out;
+}
+
+__global__ void life_unpack(const uint32_t* __restrict__ bits, uint8_t* __restrict__ cells, size_t nwords)
+{
+    size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwords) return;
+    uint32_t b = __ldg(bits + w), v[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        uint32_t x = (b >> (4 * k)) & 0xfu;
+        x = (x | (x << 14)) & 0x00030003u;
+        x = (x | (x << 7)) & LSB;
+        v[k] = x;
+    }
+    uint4* p = reinterpret_cast<uint4*>(cells + w * 32);
+    p[0] = make_uint4(v[0], v[1], v[2], v[3]);
+    p[1] = make_uint4(v[4], v[5], v[6], v[7]);
+}
+
+// Population: popcount over 32-bit words (u8 cells are 0/1, so popc of 4 bytes = live bytes).
+__global__ void popcount_words(const uint32_t* __restrict__ words, size_t n, unsigned long long* __restrict__ out)
+{
+    unsigned long long s = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        s += __popc(__ldg(words + i));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(FULL, s, o);
+    __shared__ unsigned long long part[32];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(FULL, s, o);
+        if (threadIdx.x == 0) atomicAdd(out, s);
+    }
+}
+
+// tail of a byte array whose length is not a multiple of 4
+__global__ void popcount_tail(const uint8_t* __restrict__ p, int n, unsigned long long* __restrict__ out)
+{
+    unsigned long long s = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += p[i];
+    if (s) atomicAdd(out, s);
+}
+
+template <int RULE>
+int run_u8(uint8_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStream_t st)
+{
+    int ci = 0;
+    if (nx % 16 == 0) {
+        const int strips = (nx + 511) / 512;
+        const int tasks = strips * ((ny + LIFE_ROWS - 1) / LIFE_ROWS);
+        const unsigned grid = gb::ceil_div((size_t)tasks * 32, 256);
+        for (int g = 0; g < gens; g++) {
+            life_u8_swar<RULE><<<grid, 256, 0, st>>>(buf[ci], buf[1 - ci], nx, ny, strips, tasks);
+            ci = 1 - ci;
+        }
+    } else {
+        dim3 blk(32, 8), grd(gb::ceil_div(nx, 32), gb::ceil_div(ny, 8));
+        for (int g = 0; g < gens; g++) {
+            life_u8_generic<RULE><<<grd, blk, 0, st>>>(buf[ci], buf[1 - ci], nx, ny);
+            ci = 1 - ci;
+        }
+    }
+    GB_TRY(gb::launched("life_u8 sweep"));
+    if (cur_index) *cur_index = ci;
+    return APPFIS_GB_OK;
+}
+
+template <int RULE>
+int run_bits(uint32_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStream_t st)
+{
+    const int nw = nx / 32;
+    const int strips = (nw + 31) / 32;
+    const int tasks = strips * ((ny + LIFE_ROWS - 1) / LIFE_ROWS);
+    const unsigned grid = gb::ceil_div((size_t)tasks * 32, 256);
+    int ci = 0;
+    for (int g = 0; g < gens; g++) {
+        life_bits_sweep<RULE><<<grid, 256, 0, st>>>(buf[ci], buf[1 - ci], nw, ny, strips, tasks);
+        ci = 1 - ci;
+    }
+    GB_TRY(gb::launched("life_bits sweep"));
+    if (cur_index) *cur_index = ci;
+    return APPFIS_GB_OK;
+}
+
+int check_life(const void* a, const void* b, int nx, int ny, int gens, int rule)
+{
+    if (!a || !b) return gb::fail(APPFIS_GB_EINVAL, "life: null buffer");
+    if (a == b) return gb::fail(APPFIS_GB_EINVAL, "life: the two buffers must differ");
+    if (nx < 1 || ny < 1) return gb::fail(APPFIS_GB_EINVAL, "life: bad size %d x %d", nx, ny);
+    if ((size_t)nx * (size_t)ny > ((size_t)1 << 40)) return gb::fail(APPFIS_GB_EINVAL, "life: grid too large");
+    if (gens < 0) return gb::fail(APPFIS_GB_EINVAL, "life: negative generation count");
+    if (rule != APPFIS_GB_LIFE_REFERENCE && rule != APPFIS_GB_LIFE_B3S23)
+        return gb::fail(APPFIS_GB_EINVAL, "life: unknown rule %d", rule);
+    return APPFIS_GB_OK;
+}
+
+int population_u8(const uint8_t* cells, int64_t n, int64_t* dev_count, cudaStream_t st)
+{
+    GB_CUDA(cudaMemsetAsync(dev_count, 0, sizeof(int64_t), st));
+    size_t nw = (size_t)n / 4;
+    if (nw) {
+        unsigned grid = (unsigned)std::min<size_t>(gb::ceil_div(nw, 256), (size_t)gb::sm_count() * 8);
+        popcount_words<<<grid, 256, 0, st>>>(reinterpret_cast<const uint32_t*>(cells), nw,
+                                             reinterpret_cast<unsigned long long*>(dev_count));
+    }
+    if (n % 4)
+        popcount_tail<<<1, 32, 0, st>>>(cells + nw * 4, (int)(n % 4), reinterpret_cast<unsigned long long*>(dev_count));
+    return gb::launched("life population");
+}
+
+}  // namespace
+
+extern "C" {
+
+int appfis_gb_life_u8(uint8_t* a, uint8_t* b, int nx, int ny, int gens, int rule, int* cur_index, void* stream)
+{
+    GB_TRY(check_life(a, b, nx, ny, gens, rule));
+    if (nx % 16 == 0 && ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15))
+        return gb::fail(APPFIS_GB_EINVAL, "life_u8: buffers must be 16-byte aligned");
+    uint8_t* buf[2] = {a, b};
+    cudaStream_t st = gb::as_stream(stream);
+    return rule == APPFIS_GB_LIFE_REFERENCE ? run_u8<APPFIS_GB_LIFE_REFERENCE>(buf, nx, ny, gens, cur_index, st)
+                                            : run_u8<APPFIS_GB_LIFE_B3S23>(buf, nx, ny, gens, cur_index, st);
+}
+
+int appfis_gb_life_bits(uint32_t* a, uint32_t* b, int nx, int ny, int gens, int rule, int* cur_index, void* stream)
+{
+    GB_TRY(check_life(a, b, nx, ny, gens, rule));
+    if (nx % 32) return gb::fail(APPFIS_GB_EINVAL, "life_bits: nx (%d) must be a multiple of 32", nx);
+    uint32_t* buf[2] = {a, b};
+    cudaStream_t st = gb::as_stream(stream);
+    return rule == APPFIS_GB_LIFE_REFERENCE ? run_bits<APPFIS_GB_LIFE_REFERENCE>(buf, nx, ny, gens, cur_index, st)
+                                            : run_bits<APPFIS_GB_LIFE_B3S23>(buf, nx, ny, gens, cur_index, st);
+}
+
+int appfis_gb_life_pack(const uint8_t* cells, uint32_t* bits, int nx, int ny, void* stream)
+{
+    if (!cells || !bits || nx < 1 || ny < 1 || nx % 32) return gb::fail(APPFIS_GB_EINVAL, "life_pack: bad arguments");
+    if (reinterpret_cast<uintptr_t>(cells) & 15) return gb::fail(APPFIS_GB_EINVAL, "life_pack: cells must be 16-byte aligned");
+    size_t nw = (size_t)nx * ny / 32;
+    life_pack<<<gb::ceil_div(nw, 256), 256, 0, gb::as_stream(stream)>>>(cells, bits, nw);
+    return gb::launched("life_pack");
+}
+
+int appfis_gb_life_unpack(const uint32_t* bits, uint8_t* cells, int nx, int ny, void* stream)
+{
+    if (!cells || !bits || nx < 1 || ny < 1 || nx % 32) return gb::fail(APPFIS_GB_EINVAL, "life_unpack: bad arguments");
+    if (reinterpret_cast<uintptr_t>(cells) & 15) return gb::fail(APPFIS_GB_EINVAL, "life_unpack: cells must be 16-byte aligned");
+    size_t nw = (size_t)nx * ny / 32;
+    life_unpack<<<gb::ceil_div(nw, 256), 256, 0, gb::as_stream(stream)>>>(bits, cells, nw);
+    return gb::launched("life_unpack");
+}
+
+int appfis_gb_life_population_u8(const uint8_t* cells, int64_t n, int64_t* dev_count, void* stream)
+{
+    if (!cells || !dev_count || n < 0) return gb::fail(APPFIS_GB_EINVAL, "life_population_u8: bad arguments");
+    if (reinterpret_cast<uintptr_t>(cells) & 3) return gb::fail(APPFIS_GB_EINVAL, "life_population_u8: cells must be 4-byte aligned");
+    return population_u8(cells, n, dev_count, gb::as_stream(stream));
+}
+
+int appfis_gb_life_population_bits(const uint32_t* bits, int64_t nwords, int64_t* dev_count, void* stream)
+{
+    if (!bits || !dev_count || nwords < 0) return gb::fail(APPFIS_GB_EINVAL, "life_population_bits: bad arguments");
+    cudaStream_t st = gb::as_stream(stream);
+    GB_CUDA(cudaMemsetAsync(dev_count, 0, sizeof(int64_t), st));
+    if (nwords) {
+        unsigned grid = (unsigned)std::min<size_t>(gb::ceil_div((size_t)nwords, 256), (size_t)gb::sm_count() * 8);
+        popcount_words<<<grid, 256, 0, st>>>(bits, (size_t)nwords, reinterpret_cast<unsigned long long*>(dev_count));
+    }
+    return gb::launched("life_population_bits");
+}
+
+int appfis_gb_life_job(const uint8_t* cells_in, uint8_t* cells_out, int nx, int ny, int gens, int rule, int form,
+                       int64_t* population)
+{
+    if (!cells_in) return gb::fail(APPFIS_GB_EINVAL, "life_job: null input");
+    if (form != APPFIS_GB_FORM_U8 && form != APPFIS_GB_FORM_BITS) return gb::fail(APPFIS_GB_EINVAL, "life_job: form %d", form);
+    GB_TRY(check_life(cells_in, cells_in + 1, nx, ny, gens, rule));
+    if (form == APPFIS_GB_FORM_BITS && nx % 32) return gb::fail(APPFIS_GB_EINVAL, "life_job: bit form needs nx %% 32 == 0");
+    static cudaStream_t st = nullptr;
+    if (!st) GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const size_t n = (size_t)nx * ny;
+    const size_t nbytes = (n + 15) & ~(size_t)15;
+    void *ua, *ub, *cnt;
+    GB_TRY(gb::workspace(gb::WS_JOB_A, nbytes, &ua));
+    GB_TRY(gb::workspace(gb::WS_JOB_F, 64, &cnt));
+    GB_CUDA(cudaMemcpyAsync(ua, cells_in, n, cudaMemcpyHostToDevice, st));
+    uint8_t* latest = nullptr;
+    if (form == APPFIS_GB_FORM_U8) {
+        GB_TRY(gb::workspace(gb::WS_JOB_B, nbytes, &ub));
+        GB_CUDA(cudaMemsetAsync(ub, 0, n, st));
+        int ci = 0;
+        GB_TRY(appfis_gb_life_u8((uint8_t*)ua, (uint8_t*)ub, nx, ny, gens, rule, &ci, st));
+        latest = ci == 0 ? (uint8_t*)ua : (uint8_t*)ub;
+        GB_TRY(appfis_gb_life_population_u8(latest, (int64_t)n, (int64_t*)cnt, st));
+    } else {
+        void *wa, *wb;
+        const size_t wbytes = n / 8;
+        GB_TRY(gb::workspace(gb::WS_JOB_C, wbytes, &wa));
+        GB_TRY(gb::workspace(gb::WS_JOB_D, wbytes, &wb));
+        GB_TRY(appfis_gb_life_pack((const uint8_t*)ua, (uint32_t*)wa, nx, ny, st));
+        GB_CUDA(cudaMemsetAsync(wb, 0, wbytes, st));
+        int ci = 0;
+        GB_TRY(appfis_gb_life_bits((uint32_t*)wa, (uint32_t*)wb, nx, ny, gens, rule, &ci, st));
+        uint32_t* lw = ci == 0 ? (uint32_t*)wa : (uint32_t*)wb;
+        GB_TRY(appfis_gb_life_population_bits(lw, (int64_t)(n / 32), (int64_t*)cnt, st));
+        if (cells_out) GB_TRY(appfis_gb_life_unpack(lw, (uint8_t*)ua, nx, ny, st));
+        latest = (uint8_t*)ua;
+    }
+    if (cells_out) GB_CUDA(cudaMemcpyAsync(cells_out, latest, n, cudaMemcpyDeviceToHost, st));
+    int64_t pop = 0;
+    GB_CUDA(cudaMemcpyAsync(&pop, cnt, sizeof pop, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if (population) *population = pop;
+    return APPFIS_GB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,352 @@
+"""Benchmark: GameOfLife 16384^2, 2000 generations (GLUP/s), plus per-workload lines.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one whole run of the workload: the 16384^2 u8 grid (already in HBM for `value`),
+2000 generations of the reference rule, population count.  `value` uses the bit-packed form
+(identical states to the u8 form); `e2e` is the same run through the C-ABI host-buffer entry
+point appfis_gb_life_job from pinned host memory (upload, pack, 2000 generations, unpack,
+download of the final grid and the population).  Under torchrun every rank runs its own
+replica (weak scaling); rank 0 prints one JSON line.
+
+--impl reference times the reference's own CPU path (the reference headers built with
+APPFIS_CPU, OpenMP on every host core, single-rank MPI stand-in; oracle/_ref) on a bounded
+sample of the same grid, falling back to the oracle restatement when that build is absent.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "GLUP/s + % of HBM roofline per app; batched/mixed vs plain FP32 at fixed error"
+GOL_NX = GOL_NY = 16384
+GOL_GENS = 2000
+GOL_SEED = 42
+GOL_P = 0.3
+WORKLOAD = "GameOfLife 16384x16384 u8 cells, periodic, Bernoulli(0.3) seed 42, 2000 generations, reference rule"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during a timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    parts = [x.strip() for x in line.split(",")]
+                    if len(parts) >= 9:
+                        rows.append(parts)
+            os.unlink(self.path)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------- distributed
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------- CPU baseline
+def cpu_gol_sample(cells, gens):
+    """Reference OpenMP path (oracle/_ref/ref_gol) on the full grid for `gens` generations;
+    returns (GLUP/s, cores, kind).  Falls back to the oracle restatement."""
+    from oracle import build_ref
+    from oracle import oracle as O
+
+    cores = os.cpu_count() or 1
+    ny, nx = cells.shape
+    if build_ref.exe_path("gol") is None:
+        try:
+            build_ref.build()
+        except Exception:
+            pass
+    if build_ref.exe_path("gol") is not None:
+        res, _ = O.run_ref("gol", [nx, ny, gens, cores, "{in0}", "{out0}"], [cells], [(np.uint8, 0)])
+        return nx * ny * gens / res["seconds"] / 1e9, cores, "reference"
+    t = time.perf_counter()
+    O.gol(cells, gens, threads=cores)
+    return nx * ny * gens / (time.perf_counter() - t) / 1e9, cores, "port"
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from appfis_gb300 import workloads as W
+
+    cells = W.gol_cells(GOL_NX, GOL_NY, GOL_P, GOL_SEED)
+    gens = args.ref_gens
+    vals = []
+    kind = cores = None
+    for s in range(args.warmup + args.steps):
+        v, cores, kind = cpu_gol_sample(cells, gens)
+        if s >= args.warmup:
+            vals.append(v)
+    value = statistics.mean(vals)
+    sample = "16384x16384 grid, %d generations per step (of the 2000-generation workload)" % gens
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GLUP/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": GOL_NX * GOL_NY * gens / value / 1e6,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "i32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample_generations": gens},
+            "cpu_baseline": {"value": value, "unit": "GLUP/s", "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": "GLUP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- our arm
+def run_ours(args, rank, world, local):
+    import torch
+
+    import appfis_gb300 as gb
+    from appfis_gb300 import build as gb_build
+    from appfis_gb300 import workloads as W
+
+    gb_build.build()
+    L = gb.lib()
+    hbm_peak, peak_kind = peaks()
+    N = GOL_NX * GOL_NY
+    gens = GOL_GENS
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    cells = W.gol_cells(GOL_NX, GOL_NY, GOL_P, GOL_SEED)
+    host_in = torch.from_numpy(cells).pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+    d_cells = host_in.to(dev)
+    nw = N // 32
+    wa = torch.empty(nw, dtype=torch.int32, device=dev)
+    wb = torch.empty(nw, dtype=torch.int32, device=dev)
+    ua = torch.empty(N, dtype=torch.uint8, device=dev)
+    ub = torch.empty(N, dtype=torch.uint8, device=dev)
+    cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+    ci = ctypes.c_int(0)
+
+    def step_bits():
+        gb.call("appfis_gb_life_pack", d_cells.data_ptr(), wa.data_ptr(), GOL_NX, GOL_NY, sp)
+        wb.zero_()
+        gb.call("appfis_gb_life_bits", wa.data_ptr(), wb.data_ptr(), GOL_NX, GOL_NY, gens, 0, ctypes.byref(ci), sp)
+        latest = wa if ci.value == 0 else wb
+        gb.call("appfis_gb_life_population_bits", latest.data_ptr(), nw, cnt.data_ptr(), sp)
+
+    def step_u8():
+        ua.copy_(d_cells)
+        ub.zero_()
+        gb.call("appfis_gb_life_u8", ua.data_ptr(), ub.data_ptr(), GOL_NX, GOL_NY, gens, 0, ctypes.byref(ci), sp)
+        latest = ua if ci.value == 0 else ub
+        gb.call("appfis_gb_life_population_u8", latest.data_ptr(), N, cnt.data_ptr(), sp)
+
+    def timed(step, k, w, sample_clocks=False):
+        for _ in range(w):
+            step()
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        sampler = ClockSampler(local) if sample_clocks else None
+        if sampler:
+            sampler.__enter__()
+        e0.record(stream)
+        for _ in range(k):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        if sampler:
+            sampler.__exit__()
+        barrier(world)
+        ms = max_over_ranks(e0.elapsed_time(e1), world) / k
+        return ms, (sampler.summary() if sampler else None)
+
+    # headline: bit-packed form, inputs resident in HBM
+    ms_bits, clocks = timed(step_bits, args.steps, args.warmup, sample_clocks=True)
+    population = int(cnt.item())
+    value = N * gens / (ms_bits * 1e-3) / 1e9 * world
+
+    # dominant kernel alone: the bit-packed sweep, average launch duration over G launches
+    def kernel_avg(fn_name, a, b, g):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        gb.call(fn_name, a.data_ptr(), b.data_ptr(), GOL_NX, GOL_NY, g, 0, ctypes.byref(ci), sp)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / g
+
+    gb.call("appfis_gb_life_pack", d_cells.data_ptr(), wa.data_ptr(), GOL_NX, GOL_NY, sp)
+    kernel_avg("appfis_gb_life_bits", wa, wb, 20)
+    bits_ms = kernel_avg("appfis_gb_life_bits", wa, wb, 400)
+    bits_bytes = N * 3 / 8  # read cur + read old + write new, 1 bit each
+    bits_achieved = bits_bytes / (bits_ms * 1e-3) / 1e9
+
+    # u8 form (the byte-per-cell reference layout)
+    ms_u8, _ = timed(step_u8, max(1, min(args.steps, 3)), 1)
+    pop_u8 = int(cnt.item())
+    ua.copy_(d_cells)
+    ub.zero_()
+    kernel_avg("appfis_gb_life_u8", ua, ub, 10)
+    u8_ms = kernel_avg("appfis_gb_life_u8", ua, ub, 100)
+    u8_bytes = N * 3
+    u8_achieved = u8_bytes / (u8_ms * 1e-3) / 1e9
+
+    # end to end through the C ABI from pinned host buffers
+    pop = ctypes.c_int64(0)
+
+    def step_e2e():
+        gb.call("appfis_gb_life_job", host_in.data_ptr(), host_out.data_ptr(), GOL_NX, GOL_NY, gens, 0, 1,
+                ctypes.byref(pop))
+
+    for _ in range(args.warmup):
+        step_e2e()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+    e2e_value = N * gens / e2e_s / 1e9 * world
+    assert pop.value == population == pop_u8, "forms disagree on the population"
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "GLUP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_bits, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": "bit-packed (32 cells/word), states identical to u8",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "each step starts from the 268 MB u8 grid (larger than L2); the packed state (67 MB for "
+                         "both buffers) stays L2-resident across generations within a step",
+                   "population": population},
+        "e2e": {"value": e2e_value, "unit": "GLUP/s", "h2d_bytes_per_step": N, "d2h_bytes_per_step": N + 8,
+                "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": args.steps * (gens + 2),
+        "roofline": {"bound": "hbm", "achieved": bits_achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": bits_achieved / hbm_peak, "traffic": None, "kernel": "life_bits_sweep",
+                     "algorithmic_bytes_per_launch": bits_bytes, "avg_launch_ms": bits_ms,
+                     "peak_source": peak_kind},
+        "forms": {
+            "bits": {"glups": value, "ms_per_step": ms_bits, "kernel_ms": bits_ms, "achieved_gbs": bits_achieved},
+            "u8": {"glups": N * gens / (ms_u8 * 1e-3) / 1e9 * world, "ms_per_step": ms_u8, "kernel_ms": u8_ms,
+                   "achieved_gbs": u8_achieved, "frac": u8_achieved / hbm_peak, "bytes_per_lup": 3},
+        },
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, kind = cpu_gol_sample(cells, args.ref_gens)
+        line["cpu_baseline"] = {"value": v, "unit": "GLUP/s", "cores": cores, "kind": kind,
+                                "sample": "16384x16384 grid, %d generations" % args.ref_gens}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--ref-gens", type=int, default=8, help="generations per CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,131 @@
+/*
+ * appfis_gb.h — C ABI of the GB300-native APPFIS stencil engine (libappfis_gb.so).
+ *
+ * The reference (msharif42/APPFIS) exposes its hot path as header-only C++ templates: the user
+ * writes APPFIS::Stencil overloads and calls Execute{1,2,3}D / Execute*DReduce / HaloExchange
+ * per iteration (Appfis/Runtime.hpp:23-57).  This library is what those calls land on for the
+ * five workloads: hand-written sm_103a kernels behind plain C entry points, so that the
+ * drop-in C++ headers (appfis_gb300/Appfis/) and any FFI (ctypes, cgo, JNI) can bind them.
+ *
+ * Conventions
+ *  - Every function returns a status (APPFIS_GB_OK = 0); appfis_gb_last_error() gives the
+ *    calling thread's message of the last failure.  No exception crosses the ABI.
+ *  - Device pointers are caller-owned, x-fastest, padded exactly like the reference's
+ *    sub-grids (interior + 2*ghost per axis, Appfis/Common.hpp:197-226) unless stated.
+ *    `pitch` is the row stride in elements (>= the padded x extent).
+ *  - `stream` is a cudaStream_t (NULL = the legacy default stream).  Device entry points are
+ *    asynchronous on that stream; results that land in host memory (suffix _job, *_host)
+ *    synchronise it.
+ *  - Two-buffer iterations (the reference's DUAL grids, Appfis/Grid.hpp:367-397) take both
+ *    buffers and report in *cur_index which one holds the newest state (0 = a, 1 = b), which
+ *    is what Grid::Swap tracks in the reference (Appfis/Grid.hpp:854-857).
+ *  - Entry points with the suffix _job take HOST buffers and run a whole workload end to end
+ *    (upload, iterate, download) on an internal stream with reused device workspace; calls
+ *    from several host threads to the same _job function must be serialised by the caller.
+ */
+#ifndef APPFIS_GB_H
+#define APPFIS_GB_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define APPFIS_GB_API __attribute__((visibility("default")))
+#else
+#define APPFIS_GB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define APPFIS_GB_OK 0
+#define APPFIS_GB_EINVAL 1       /* bad argument: null pointer, size, pitch, unsupported combination */
+#define APPFIS_GB_ECUDA 2        /* a CUDA runtime call or kernel launch failed */
+#define APPFIS_GB_ENOMEM 3       /* device or pinned host allocation failed */
+#define APPFIS_GB_ETIMEOUT 4     /* a bounded device-side wait gave up (no hang; context still usable) */
+
+/* element types (reference Scatter/AllReduce support int, float, double: Communication.hpp:66-83) */
+#define APPFIS_GB_F32 0
+#define APPFIS_GB_F64 1
+#define APPFIS_GB_I32 2
+
+/* reduction operators, same order as the reference enum REDUCTION { MAX, MIN, SUM } (Appfis/Env.hpp:32) */
+#define APPFIS_GB_MAX 0
+#define APPFIS_GB_MIN 1
+#define APPFIS_GB_SUM 2
+
+/* ----------------------------------------------------------------------------- runtime */
+APPFIS_GB_API const char* appfis_gb_last_error(void);
+APPFIS_GB_API int appfis_gb_version(void);
+/* Blocks until all work on `stream` is done (replaces the reference's cudaStreamSynchronize
+ * calls on its one stream, Appfis/Topology.hpp:151). */
+APPFIS_GB_API int appfis_gb_stream_sync(void* stream);
+
+/* ----------------------------------------------------------------------------- reductions */
+/* Execute{1,2,3}DReduce over a box (Appfis/Runtime.hpp:225-255 dispatch; GPU path
+ * Appfis/Runtime_CUDA.hpp:554-740; CPU path Runtime.hpp:597-913; AllReduce Communication.hpp:752-789).
+ * field: padded device field of type `dtype` with x pitch `px` and y extent `py` (rows per plane);
+ * box = {x0, x1, y0, y1, z0, z1}, half-open (a Config's [start, end) per axis; use {0,1} for absent axes).
+ * The result is written to the 8-byte device location dev_result: a double for F32/F64, an
+ * int64 for I32.  MAX is seeded with std::numeric_limits<T>::min() like the reference (for
+ * floating types that is the smallest positive normal, so an all-negative box returns it),
+ * MIN with max(), SUM with 0.  Floating SUMs accumulate in double; every result is deterministic
+ * (fixed-order tree: per-block partials, then the last block folds them in block order). */
+APPFIS_GB_API int appfis_gb_reduce(const void* field, int dtype, int px, int py, const int* box, int op, void* dev_result,
+                     void* stream);
+/* Same, returning the value on the host (synchronises `stream`). */
+APPFIS_GB_API int appfis_gb_reduce_host(const void* field, int dtype, int px, int py, const int* box, int op, double* result,
+                          void* stream);
+
+/* ----------------------------------------------------------------------------- GameOfLife */
+/* Replaces Execute2D(config, cur, next) with the GameOfLife functor + the periodic halo
+ * exchange per generation (GameOfLife/src/game_appfis.hpp:79-82,121-135;
+ * Appfis/Runtime_CUDA.hpp:345-369; Appfis/Communication.hpp:612-678).
+ * Cells are u8 0/1 on the nx*ny INTERIOR only (row pitch nx): the periodic ghost ring of the
+ * reference is not stored, the kernels wrap indices instead.
+ * rule APPFIS_GB_LIFE_REFERENCE: the reference rule — a live cell dies when its count is < 2 or
+ *   > 4, a dead cell is born when the count is 3, and otherwise the output buffer is left as it
+ *   was (it then holds the state of two generations back).  Both buffers are read.
+ * rule APPFIS_GB_LIFE_B3S23: Conway's B3/S23, a different function (not the reference's).
+ * a = state at t, b = state at t-1 (zeros for the first call, as the reference zero-fills). */
+#define APPFIS_GB_LIFE_REFERENCE 0
+#define APPFIS_GB_LIFE_B3S23 1
+APPFIS_GB_API int appfis_gb_life_u8(uint8_t* a, uint8_t* b, int nx, int ny, int gens, int rule, int* cur_index, void* stream);
+/* Bit-packed form: 32 cells per uint32 word, bit k of word w of row j = cell (32w + k, j);
+ * nx must be a multiple of 32.  States are identical to appfis_gb_life_u8. */
+APPFIS_GB_API int appfis_gb_life_pack(const uint8_t* cells, uint32_t* bits, int nx, int ny, void* stream);
+APPFIS_GB_API int appfis_gb_life_unpack(const uint32_t* bits, uint8_t* cells, int nx, int ny, void* stream);
+APPFIS_GB_API int appfis_gb_life_bits(uint32_t* a, uint32_t* b, int nx, int ny, int gens, int rule, int* cur_index, void* stream);
+/* Population (Execute2DReduce SUM of the cells, game_appfis.hpp:84) into an int64 device location. */
+APPFIS_GB_API int appfis_gb_life_population_u8(const uint8_t* cells, int64_t n, int64_t* dev_count, void* stream);
+APPFIS_GB_API int appfis_gb_life_population_bits(const uint32_t* bits, int64_t nwords, int64_t* dev_count, void* stream);
+/* Whole run from host buffers: cells_in (nx*ny u8) -> cells_out (nx*ny u8, may alias cells_in)
+ * after `gens` generations; *population = live cells at the end.  form 0 = u8 kernels,
+ * 1 = bit-packed kernels (nx % 32 == 0).  A NULL cells_out skips the field download. */
+#define APPFIS_GB_FORM_U8 0
+#define APPFIS_GB_FORM_BITS 1
+APPFIS_GB_API int appfis_gb_life_job(const uint8_t* cells_in, uint8_t* cells_out, int nx, int ny, int gens, int rule, int form,
+                       int64_t* population);
+
+/* ----------------------------------------------------------------------------- Heat (2-D) */
+/* Replaces the per-iteration Execute2D(config, cx, cy, cur, next) of the heat functor
+ * (HeatDiffusion/src/heat_appfis.hpp:87-90,166-174, restated in 2-D FP32) on a DUAL grid with a
+ * Dirichlet ghost ring (Grid::SetBoundary, Appfis/Grid.hpp:529-678) held in both buffers.
+ * a, b: padded (nx+2) x (ny+2) fields with row pitch `pitch`; the update is
+ *   next = c + cx*((l + r) - 2c) + cy*((u + d) - 2c)
+ * evaluated with the same rounding sequence as the reference CPU path (no FMA contraction), so
+ * results are bit-identical to it.  `iters` sweeps run as time-blocked launches (several sweeps
+ * per launch in shared memory) with the identical per-point arithmetic. */
+APPFIS_GB_API int appfis_gb_heat2d(float* a, float* b, int nx, int ny, int pitch, int iters, float cx, float cy, int* cur_index,
+                     void* stream);
+/* One sweep per launch (the plain form; also what the drop-in Execute2D registration uses). */
+APPFIS_GB_API int appfis_gb_heat2d_sweep(const float* cur, float* next, int nx, int ny, int pitch, float cx, float cy, void* stream);
+/* Whole run from host: field is the padded (nx+2)*(ny+2) dense array (ghost ring included), in
+ * place.  stats (optional, 3 doubles): MAX, MIN, SUM of the interior at the end (reference seeds). */
+APPFIS_GB_API int appfis_gb_heat2d_job(float* field, int nx, int ny, int iters, float cx, float cy, double* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* APPFIS_GB_H */
