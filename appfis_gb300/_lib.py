@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "libappfis_gb.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "appfis_gb.h")
 
 OK, EINVAL, ECUDA, ENOMEM, ETIMEOUT = 0, 1, 2, 3, 4
-F32, F64, I32 = 0, 1, 2
+F32, F64, I32, F16 = 0, 1, 2, 3
 MAX, MIN, SUM = 0, 1, 2
 LIFE_REFERENCE, LIFE_B3S23 = 0, 1
 FORM_U8, FORM_BITS = 0, 1
@@ -40,7 +40,50 @@ SIGNATURES = {
     "appfis_gb_heat2d": [_P, _P, _i, _i, _i, _i, _f, _f, _P, _P],
     "appfis_gb_heat2d_sweep": [_P, _P, _i, _i, _i, _f, _f, _P],
     "appfis_gb_heat2d_job": [_P, _i, _i, _i, _f, _f, _P],
+    "appfis_gb_himeno": [_P, _P, _P, _i, _i, _i, _i, _i, _f, _P, _P, _P],
+    "appfis_gb_himeno_mixed": [_P, _P, _P, _P, _i, _i, _i, _i, _i, _i, _f, _P, _P, _P],
+    "appfis_gb_himeno_job": [_P, _P, _i, _i, _i, _i, _f, _i, _i, _P],
+    "appfis_gb_star_r4": [_P, _P, _i, _i, _i, _i, _i, _i, _i, _f, _P, _i, _i, _P, _P],
+    "appfis_gb_flood_run": [_P, _i, _i, _P, _P, _P, _P, _P, _P],
+    "appfis_gb_flood_job": [_i, _P, _P, _P, _P, _P, _P, _d, _P, _i, _P, _P, _P],
 }
+
+
+class FloodDomain(ctypes.Structure):
+    """appfis_gb_flood_domain"""
+    _fields_ = [("nx", _i), ("ny", _i), ("pitch", _i), ("h", _P * 2), ("qx", _P * 2), ("qy", _P * 2),
+                ("dem", _P), ("n2", _P)]
+
+
+class FloodParams(ctypes.Structure):
+    """appfis_gb_flood_params"""
+    _fields_ = [("dx", _d), ("courant", _d), ("hextra", _d), ("t_end", _d), ("print_interval", _d),
+                ("time_step", _d), ("t_start", _d), ("max_steps", _i)]
+
+
+def flood_job(domains, dx, courant, hextra, manning, t_end, print_interval=None, time_step=1.0, max_steps=0,
+              dtype=F32, qx=None, qy=None):
+    """Run a batch of flood domains from host arrays.  domains: list of (dem, h) FP64 (ny, nx)
+    arrays.  Returns dict(h=[...], qx=[...], qy=[...], steps=[...], mass=[(m0, m1)], dts=[...])."""
+    import numpy as np
+    nd = len(domains)
+    nx = (_i * nd)(*[d[0].shape[1] for d in domains])
+    ny = (_i * nd)(*[d[0].shape[0] for d in domains])
+    dems = [np.ascontiguousarray(d[0], dtype=np.float64) for d in domains]
+    hs = [np.ascontiguousarray(d[1], dtype=np.float64).copy() for d in domains]
+    qxs = [np.zeros_like(a) if qx is None else np.ascontiguousarray(qx[k], dtype=np.float64).copy() for k, a in enumerate(hs)]
+    qys = [np.zeros_like(a) if qy is None else np.ascontiguousarray(qy[k], dtype=np.float64).copy() for k, a in enumerate(hs)]
+    P = lambda arrs: (_P * nd)(*[a.ctypes.data for a in arrs])
+    prm = FloodParams(dx, courant, hextra, t_end, t_end if print_interval is None else print_interval, time_step, 0.0,
+                      max_steps)
+    steps = (_i * nd)()
+    mass = (_d * (2 * nd))()
+    dtlog = np.zeros(nd * max(max_steps, 1), dtype=np.float64)
+    call("appfis_gb_flood_job", nd, nx, ny, P(dems), P(hs), P(qxs), P(qys), manning, ctypes.byref(prm), dtype, steps,
+         mass, dtlog.ctypes.data if max_steps > 0 else None)
+    st = list(steps)
+    return dict(h=hs, qx=qxs, qy=qys, steps=st, mass=[(mass[2 * k], mass[2 * k + 1]) for k in range(nd)],
+                dts=[dtlog[k * max_steps:k * max_steps + st[k]] for k in range(nd)] if max_steps > 0 else None)
 _RESTYPES = {"appfis_gb_last_error": ctypes.c_char_p}
 
 

@@ -20,6 +20,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libappfis_gb.so")
 INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# per-file extra flags: the FP64 flood model keeps the reference's separate multiply/add rounding
+PER_FILE_FLAGS = {"flood_f64.cu": ["-fmad=false"]}
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC]
 
@@ -44,7 +46,7 @@ def _compile(src, force, verbose):
     obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
     if not force and os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), _deps_mtime()):
         return obj
-    cmd = [_nvcc()] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj]
+    cmd = [_nvcc()] + ARCH + NVCC_FLAGS + PER_FILE_FLAGS.get(os.path.basename(src), []) + ["-c", src, "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,0 +1,346 @@
+// Himeno 19-point Jacobi (FP32 plain form and FP16-storage defect-correction form), with the
+// per-sweep gosa = sum(ss^2) reduced in double inside the sweep.
+//
+// Reference functor: Himeno/src/himeno_appfis.hpp:178-198, run by Execute3D once per iteration
+// on a DUAL p grid and 12 SINGLE coefficient grids (:74-86, :108-114).  The reference computes
+// no gosa; ss is exactly its :195 expression.
+//
+// Plain form: one launch per sweep.  A thread owns an (i, j) column and marches a chunk of z,
+// carrying p(k-1), p(k), p(k+1) in registers; the other 14 p neighbours come through L1.  The
+// 12 coefficient streams are read once.  The sum uses round-to-nearest intrinsics in the
+// reference's order (no FMA contraction), so p is bit-identical to the reference CPU path.
+//
+// Defect-correction form (FP16 storage, FP32 arithmetic).  With p = P + e (P an FP32 master
+// frozen between corrections) the Jacobi update p' = p + w*bnd*(a3*(N p + wrk1) - p) becomes
+//     e' = Wc*e + sum_n Wn*(e neighbour terms) + D,   Wc = 1 - w*bnd,  Wn = w*bnd*a3*coef_n,
+//     D  = w*ss(P)   (the FP32 defect of the master),
+// an exact rewrite.  Inner sweeps read e, D and the 10 folded weights in FP16 (26 B per point
+// instead of 56).  Every `period` sweeps a correction pass folds e into P, recomputes D from
+// the FP32 coefficients and restarts e at 0, which bounds the FP16 error to the last period's
+// correction.  The sweep's own ss is (e' - e)/w (FP32, before rounding e').
+#include <cuda_fp16.h>
+
+#include "gb_common.cuh"
+
+namespace {
+
+struct Coef12 {
+    const float* c[12];  // a0 a1 a2 a3 b0 b1 b2 c0 c1 c2 bnd wrk1
+};
+struct W10 {
+    const __half* w[10];  // xp yp zp b0 b1 b2 xm ym zm centre
+};
+
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+
+// Deterministic block sum of v, then the last block folds all partials into *out.
+__device__ __forceinline__ void gosa_reduce(double v, double* __restrict__ partials, unsigned* __restrict__ ticket,
+                                            double* __restrict__ out)
+{
+    __shared__ double sh[32];
+    __shared__ bool last;
+    const int nthreads = blockDim.x * blockDim.y;
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((t & 31) == 0) sh[t >> 5] = v;
+    __syncthreads();
+    const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned b = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    if (t < 32) {
+        v = t < (nthreads >> 5) ? sh[t] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (t == 0) {
+            partials[b] = v;
+            __threadfence();
+            last = atomicAdd(ticket, 1u) == nblk - 1;
+        }
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double w = 0.0;
+    for (unsigned q = t; q < nblk; q += nthreads) w += ((volatile double*)partials)[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+    __syncthreads();
+    if ((t & 31) == 0) sh[t >> 5] = w;
+    __syncthreads();
+    if (t == 0) {
+        double s = 0.0;
+        for (int q = 0; q < (nthreads >> 5); q++) s += sh[q];
+        *out = s;
+        *ticket = 0;
+    }
+}
+
+// 19-point s0 in the reference's order, on any readable field F (F(di,dj,dk) -> float)
+#define HIMENO_S0(F, A0, A1, A2, B0, B1, B2, C0, C1, C2, W1)                                               \
+    fadd(fadd(fadd(fadd(fadd(fadd(fadd(fadd(fadd(fmul(A0, F(1, 0, 0)), fmul(A1, F(0, 1, 0))), fmul(A2, F(0, 0, 1))), \
+                                           fmul(B0, fadd(fsub(fsub(F(1, 1, 0), F(1, -1, 0)), F(-1, 1, 0)), F(-1, -1, 0)))), \
+                                      fmul(B1, fadd(fsub(fsub(F(0, 1, 1), F(0, -1, 1)), F(0, 1, -1)), F(0, -1, -1)))),      \
+                                 fmul(B2, fadd(fsub(fsub(F(1, 0, 1), F(-1, 0, 1)), F(1, 0, -1)), F(-1, 0, -1)))),           \
+                            fmul(C0, F(-1, 0, 0))),                                                                         \
+                       fmul(C1, F(0, -1, 0))),                                                                              \
+                  fmul(C2, F(0, 0, -1))),                                                                                   \
+         W1)
+
+template <int BX, int BY>
+__global__ void __launch_bounds__(BX* BY) himeno_sweep(Coef12 cf, const float* __restrict__ p, float* __restrict__ out,
+                                                        int nx, int ny, int nz, int px, int py, int kz, float omega,
+                                                        double* __restrict__ partials, unsigned* __restrict__ ticket,
+                                                        double* __restrict__ gosa)
+{
+    const int i = 1 + blockIdx.x * BX + threadIdx.x;
+    const int j = 1 + blockIdx.y * BY + threadIdx.y;
+    const int k0 = 1 + blockIdx.z * kz, k1 = min(k0 + kz, nz + 1);
+    const size_t plane = (size_t)px * py;
+    double g = 0.0;
+    if (i <= nx && j <= ny) {
+        size_t c = ((size_t)k0 * py + j) * px + i;
+        float pm = __ldg(p + c - plane), p0 = __ldg(p + c);
+        for (int k = k0; k < k1; k++) {
+            const float pp = __ldg(p + c + plane);
+#define PF(di, dj, dk)                                                                                             \
+    ((di) == 0 && (dj) == 0 ? ((dk) < 0 ? pm : ((dk) > 0 ? pp : p0))                                              \
+                            : __ldg(p + c + (ptrdiff_t)(di) + (ptrdiff_t)(dj) * px + (ptrdiff_t)(dk) * (ptrdiff_t)plane))
+            const float s0 = HIMENO_S0(PF, __ldg(cf.c[0] + c), __ldg(cf.c[1] + c), __ldg(cf.c[2] + c), __ldg(cf.c[4] + c),
+                                       __ldg(cf.c[5] + c), __ldg(cf.c[6] + c), __ldg(cf.c[7] + c), __ldg(cf.c[8] + c),
+                                       __ldg(cf.c[9] + c), __ldg(cf.c[11] + c));
+#undef PF
+            const float ss = fmul(fsub(fmul(s0, __ldg(cf.c[3] + c)), p0), __ldg(cf.c[10] + c));
+            out[c] = fadd(p0, fmul(omega, ss));
+            g += (double)ss * (double)ss;
+            pm = p0;
+            p0 = pp;
+            c += plane;
+        }
+    }
+    if (gosa) gosa_reduce(g, partials, ticket, gosa);
+}
+
+// ---------------------------------------------------------------- defect-correction form
+// Folded FP16 weights from the FP32 coefficients (over the interior; ghosts stay 0).
+__global__ void himeno_fold_weights(Coef12 cf, __half* __restrict__ w, size_t field, int nx, int ny, int nz, int px,
+                                    int py, float omega)
+{
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y;
+    const int k = 1 + blockIdx.z;
+    if (i > nx) return;
+    const size_t c = ((size_t)k * py + j) * px + i;
+    const float wb = omega * cf.c[10][c];
+    const float s = wb * cf.c[3][c];
+    const int map[9] = {0, 1, 2, 4, 5, 6, 7, 8, 9};  // xp yp zp b0 b1 b2 xm ym zm
+#pragma unroll
+    for (int n = 0; n < 9; n++) w[n * field + c] = __float2half_rn(s * cf.c[map[n]][c]);
+    w[9 * field + c] = __float2half_rn(1.0f - wb);
+}
+
+// Correction pass: P' = P + e, D = omega*ss(P'), e_next = 0.  Reads P and e at neighbours.
+template <int BX, int BY>
+__global__ void __launch_bounds__(BX* BY) himeno_correct(Coef12 cf, const float* __restrict__ P, const __half* __restrict__ e,
+                                                          float* __restrict__ Pn, __half* __restrict__ D,
+                                                          __half* __restrict__ ezero, int nx, int ny, int nz, int px,
+                                                          int py, int kz, float omega)
+{
+    const int i = 1 + blockIdx.x * BX + threadIdx.x;
+    const int j = 1 + blockIdx.y * BY + threadIdx.y;
+    const int k0 = 1 + blockIdx.z * kz, k1 = min(k0 + kz, nz + 1);
+    if (i > nx || j > ny) return;
+    const size_t plane = (size_t)px * py;
+    size_t c = ((size_t)k0 * py + j) * px + i;
+    for (int k = k0; k < k1; k++) {
+#define QF(di, dj, dk)                                                                                      \
+    (__ldg(P + c + (ptrdiff_t)(di) + (ptrdiff_t)(dj) * px + (ptrdiff_t)(dk) * (ptrdiff_t)plane) +          \
+     __half2float(e[c + (ptrdiff_t)(di) + (ptrdiff_t)(dj) * px + (ptrdiff_t)(dk) * (ptrdiff_t)plane]))
+        const float q0 = QF(0, 0, 0);
+        const float s0 = HIMENO_S0(QF, __ldg(cf.c[0] + c), __ldg(cf.c[1] + c), __ldg(cf.c[2] + c), __ldg(cf.c[4] + c),
+                                   __ldg(cf.c[5] + c), __ldg(cf.c[6] + c), __ldg(cf.c[7] + c), __ldg(cf.c[8] + c),
+                                   __ldg(cf.c[9] + c), __ldg(cf.c[11] + c));
+#undef QF
+        const float ss = (s0 * __ldg(cf.c[3] + c) - q0) * __ldg(cf.c[10] + c);
+        Pn[c] = q0;
+        D[c] = __float2half_rn(omega * ss);
+        ezero[c] = __float2half_rn(0.0f);
+        c += plane;
+    }
+}
+
+template <int BX, int BY>
+__global__ void __launch_bounds__(BX* BY) himeno_inner(W10 wf, const __half* __restrict__ e, const __half* __restrict__ D,
+                                                        __half* __restrict__ en, int nx, int ny, int nz, int px, int py,
+                                                        int kz, float inv_omega, double* __restrict__ partials,
+                                                        unsigned* __restrict__ ticket, double* __restrict__ gosa)
+{
+    const int i = 1 + blockIdx.x * BX + threadIdx.x;
+    const int j = 1 + blockIdx.y * BY + threadIdx.y;
+    const int k0 = 1 + blockIdx.z * kz, k1 = min(k0 + kz, nz + 1);
+    const size_t plane = (size_t)px * py;
+    double g = 0.0;
+    if (i <= nx && j <= ny) {
+        size_t c = ((size_t)k0 * py + j) * px + i;
+        float em = __half2float(e[c - plane]), e0 = __half2float(e[c]);
+        for (int k = k0; k < k1; k++) {
+            const float ep = __half2float(e[c + plane]);
+#define EF(di, dj, dk)                                            \
+    ((di) == 0 && (dj) == 0 ? ((dk) < 0 ? em : ((dk) > 0 ? ep : e0)) \
+                            : __half2float(e[c + (ptrdiff_t)(di) + (ptrdiff_t)(dj) * px + (ptrdiff_t)(dk) * (ptrdiff_t)plane]))
+#define WF(n) __half2float(wf.w[n][c])
+            float v = WF(9) * e0 + __half2float(D[c]);
+            v += WF(0) * EF(1, 0, 0) + WF(1) * EF(0, 1, 0) + WF(2) * EF(0, 0, 1);
+            v += WF(3) * ((EF(1, 1, 0) - EF(1, -1, 0)) - (EF(-1, 1, 0) - EF(-1, -1, 0)));
+            v += WF(4) * ((EF(0, 1, 1) - EF(0, -1, 1)) - (EF(0, 1, -1) - EF(0, -1, -1)));
+            v += WF(5) * ((EF(1, 0, 1) - EF(-1, 0, 1)) - (EF(1, 0, -1) - EF(-1, 0, -1)));
+            v += WF(6) * EF(-1, 0, 0) + WF(7) * EF(0, -1, 0) + WF(8) * EF(0, 0, -1);
+#undef EF
+#undef WF
+            en[c] = __float2half_rn(v);
+            const float ss = (v - e0) * inv_omega;
+            g += (double)ss * (double)ss;
+            em = e0;
+            e0 = ep;
+            c += plane;
+        }
+    }
+    if (gosa) gosa_reduce(g, partials, ticket, gosa);
+}
+
+constexpr int HBX = 32, HBY = 4, HKZ = 32;
+
+int check_dims(int nx, int ny, int nz, int pitch)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || pitch < nx + 2) return gb::fail(APPFIS_GB_EINVAL, "himeno: bad dims %d %d %d pitch %d", nx, ny, nz, pitch);
+    if ((size_t)pitch * (ny + 2) * (nz + 2) > ((size_t)1 << 36)) return gb::fail(APPFIS_GB_EINVAL, "himeno: grid too large");
+    return APPFIS_GB_OK;
+}
+
+int gosa_scratch(dim3 grd, double** partials, unsigned** ticket, cudaStream_t st)
+{
+    void* ws;
+    const size_t nblk = (size_t)grd.x * grd.y * grd.z;
+    GB_TRY(gb::workspace(gb::WS_REDUCE, 256 + sizeof(double) * nblk, &ws));
+    *ticket = reinterpret_cast<unsigned*>(ws);
+    *partials = reinterpret_cast<double*>(reinterpret_cast<char*>(ws) + 256);
+    GB_CUDA(cudaMemsetAsync(*ticket, 0, sizeof(unsigned), st));
+    return APPFIS_GB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int appfis_gb_himeno(const float* const* coef, float* p, float* wrk2, int nx, int ny, int nz, int pitch, int iters,
+                     float omega, double* dev_gosa, int* cur_index, void* stream)
+{
+    if (!coef || !p || !wrk2 || p == wrk2) return gb::fail(APPFIS_GB_EINVAL, "himeno: null or aliased buffers");
+    for (int n = 0; n < 12; n++)
+        if (!coef[n]) return gb::fail(APPFIS_GB_EINVAL, "himeno: coefficient %d is null", n);
+    GB_TRY(check_dims(nx, ny, nz, pitch));
+    if (iters < 0) return gb::fail(APPFIS_GB_EINVAL, "himeno: negative iteration count");
+    cudaStream_t st = gb::as_stream(stream);
+    Coef12 cf;
+    for (int n = 0; n < 12; n++) cf.c[n] = coef[n];
+    dim3 blk(HBX, HBY), grd(gb::ceil_div(nx, HBX), gb::ceil_div(ny, HBY), gb::ceil_div(nz, HKZ));
+    double* partials = nullptr;
+    unsigned* ticket = nullptr;
+    if (dev_gosa) GB_TRY(gosa_scratch(grd, &partials, &ticket, st));
+    float* buf[2] = {p, wrk2};
+    int ci = 0;
+    for (int it = 0; it < iters; it++) {
+        himeno_sweep<HBX, HBY><<<grd, blk, 0, st>>>(cf, buf[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2, HKZ, omega, partials,
+                                                    ticket, dev_gosa ? dev_gosa + it : nullptr);
+        ci = 1 - ci;
+    }
+    GB_TRY(gb::launched("himeno_sweep"));
+    if (cur_index) *cur_index = ci;
+    return APPFIS_GB_OK;
+}
+
+int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, void* half_work, int nx, int ny, int nz,
+                           int pitch, int iters, int period, float omega, double* dev_gosa, int* cur_index, void* stream)
+{
+    if (!coef || !p || !p_work || !half_work || p == p_work) return gb::fail(APPFIS_GB_EINVAL, "himeno_mixed: null or aliased buffers");
+    for (int n = 0; n < 12; n++)
+        if (!coef[n]) return gb::fail(APPFIS_GB_EINVAL, "himeno_mixed: coefficient %d is null", n);
+    GB_TRY(check_dims(nx, ny, nz, pitch));
+    if (iters < 0 || period < 1) return gb::fail(APPFIS_GB_EINVAL, "himeno_mixed: bad iters %d / period %d", iters, period);
+    if (omega == 0.0f) return gb::fail(APPFIS_GB_EINVAL, "himeno_mixed: omega must be non-zero");
+    cudaStream_t st = gb::as_stream(stream);
+    const size_t field = (size_t)pitch * (ny + 2) * (nz + 2);
+    __half* hw = reinterpret_cast<__half*>(half_work);
+    __half* W = hw;                   // 10 fields
+    __half* E[2] = {hw + 10 * field, hw + 11 * field};
+    __half* Dd = hw + 12 * field;
+    Coef12 cf;
+    for (int n = 0; n < 12; n++) cf.c[n] = coef[n];
+    W10 wf;
+    for (int n = 0; n < 10; n++) wf.w[n] = W + n * field;
+    GB_CUDA(cudaMemsetAsync(hw, 0, sizeof(__half) * 13 * field, st));
+    GB_CUDA(cudaMemsetAsync(p_work, 0, sizeof(float) * field, st));
+    himeno_fold_weights<<<dim3(gb::ceil_div(nx, 128), ny, nz), 128, 0, st>>>(cf, W, field, nx, ny, nz, pitch, ny + 2, omega);
+    dim3 blk(HBX, HBY), grd(gb::ceil_div(nx, HBX), gb::ceil_div(ny, HBY), gb::ceil_div(nz, HKZ));
+    double* partials = nullptr;
+    unsigned* ticket = nullptr;
+    if (dev_gosa) GB_TRY(gosa_scratch(grd, &partials, &ticket, st));
+    float* P[2] = {p, p_work};
+    int pc = 0, ec = 0;
+    // D from the initial P (e = 0), e restarted at 0
+    himeno_correct<HBX, HBY><<<grd, blk, 0, st>>>(cf, P[pc], E[ec], P[1 - pc], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2, HKZ, omega);
+    pc = 1 - pc;
+    ec = 1 - ec;
+    const float inv_omega = 1.0f / omega;
+    for (int it = 0; it < iters; it++) {
+        himeno_inner<HBX, HBY><<<grd, blk, 0, st>>>(wf, E[ec], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2, HKZ, inv_omega,
+                                                    partials, ticket, dev_gosa ? dev_gosa + it : nullptr);
+        ec = 1 - ec;
+        if ((it + 1) % period == 0 || it + 1 == iters) {
+            himeno_correct<HBX, HBY><<<grd, blk, 0, st>>>(cf, P[pc], E[ec], P[1 - pc], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2,
+                                                          HKZ, omega);
+            pc = 1 - pc;
+            ec = 1 - ec;
+        }
+    }
+    GB_TRY(gb::launched("himeno_mixed"));
+    if (cur_index) *cur_index = pc;
+    return APPFIS_GB_OK;
+}
+
+int appfis_gb_himeno_job(const float* coef_host, float* p_host, int nx, int ny, int nz, int iters, float omega, int form,
+                         int period, double* gosa_host)
+{
+    if (!coef_host || !p_host) return gb::fail(APPFIS_GB_EINVAL, "himeno_job: null input");
+    if (form != 0 && form != 1) return gb::fail(APPFIS_GB_EINVAL, "himeno_job: form %d", form);
+    GB_TRY(check_dims(nx, ny, nz, nx + 2));
+    static cudaStream_t st = nullptr;
+    if (!st) GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const size_t field = (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+    void *dc, *da, *db, *dh, *dg;
+    GB_TRY(gb::workspace(gb::WS_JOB_A, sizeof(float) * 12 * field, &dc));
+    GB_TRY(gb::workspace(gb::WS_JOB_B, sizeof(float) * field, &da));
+    GB_TRY(gb::workspace(gb::WS_JOB_C, sizeof(float) * field, &db));
+    GB_TRY(gb::workspace(gb::WS_JOB_E, sizeof(double) * (iters > 0 ? iters : 1), &dg));
+    GB_CUDA(cudaMemcpyAsync(dc, coef_host, sizeof(float) * 12 * field, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(da, p_host, sizeof(float) * field, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(db, da, sizeof(float) * field, cudaMemcpyDeviceToDevice, st));  // ghost ring in both
+    const float* cp[12];
+    for (int n = 0; n < 12; n++) cp[n] = reinterpret_cast<const float*>(dc) + n * field;
+    int ci = 0;
+    if (form == 0) {
+        GB_TRY(appfis_gb_himeno(cp, (float*)da, (float*)db, nx, ny, nz, nx + 2, iters, omega, gosa_host ? (double*)dg : nullptr,
+                                &ci, st));
+    } else {
+        GB_TRY(gb::workspace(gb::WS_JOB_D, sizeof(__half) * 13 * field, &dh));
+        GB_TRY(appfis_gb_himeno_mixed(cp, (float*)da, (float*)db, dh, nx, ny, nz, nx + 2, iters, period, omega,
+                                      gosa_host ? (double*)dg : nullptr, &ci, st));
+    }
+    GB_CUDA(cudaMemcpyAsync(p_host, ci == 0 ? da : db, sizeof(float) * field, cudaMemcpyDeviceToHost, st));
+    if (gosa_host && iters > 0) GB_CUDA(cudaMemcpyAsync(gosa_host, dg, sizeof(double) * iters, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    return APPFIS_GB_OK;
+}
+
+}  // extern "C"

@@ -204,7 +204,7 @@ def run_ours(args, rank, world, local):
     cells = W.gol_cells(GOL_NX, GOL_NY, GOL_P, GOL_SEED)
     host_in = torch.from_numpy(cells).pin_memory()
     host_out = torch.empty_like(host_in).pin_memory()
-    d_cells = host_in.to(dev)
+    d_cells = host_in.to(dev).view(-1)
     nw = N // 32
     wa = torch.empty(nw, dtype=torch.int32, device=dev)
     wb = torch.empty(nw, dtype=torch.int32, device=dev)
@@ -328,6 +328,29 @@ def run_ours(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def profile_case(name, local):
+    """Short fixed launch sequences for ncu captures: 16384^2 GameOfLife, 20 bit-packed sweeps
+    then 20 u8 sweeps (kernel order: life_pack, life_bits_sweep x20, life_u8_swar x20)."""
+    import torch
+
+    import appfis_gb300 as gb
+    from appfis_gb300 import workloads as W
+
+    dev = torch.device("cuda", local)
+    cells = torch.from_numpy(W.gol_cells(GOL_NX, GOL_NY, GOL_P, GOL_SEED)).to(dev).view(-1)
+    N = GOL_NX * GOL_NY
+    wa = torch.empty(N // 32, dtype=torch.int32, device=dev)
+    wb = torch.zeros_like(wa)
+    ub = torch.zeros_like(cells)
+    ci = ctypes.c_int(0)
+    sp = torch.cuda.current_stream(dev).cuda_stream
+    gb.call("appfis_gb_life_pack", cells.data_ptr(), wa.data_ptr(), GOL_NX, GOL_NY, sp)
+    gb.call("appfis_gb_life_bits", wa.data_ptr(), wb.data_ptr(), GOL_NX, GOL_NY, 20, 0, ctypes.byref(ci), sp)
+    gb.call("appfis_gb_life_u8", cells.data_ptr(), ub.data_ptr(), GOL_NX, GOL_NY, 20, 0, ctypes.byref(ci), sp)
+    torch.cuda.synchronize(dev)
+    print("profile case %s done" % name)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -336,10 +359,14 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ref-gens", type=int, default=8, help="generations per CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", choices=["life"], default=None,
+                    help="launch a short fixed sequence of the named workload's kernels (for ncu), no timing")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_setup(args.gpus)
-    if args.impl == "reference":
+    if args.profile_case:
+        profile_case(args.profile_case, local)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world, local)

@@ -43,11 +43,13 @@ extern "C" {
 #define APPFIS_GB_ECUDA 2        /* a CUDA runtime call or kernel launch failed */
 #define APPFIS_GB_ENOMEM 3       /* device or pinned host allocation failed */
 #define APPFIS_GB_ETIMEOUT 4     /* a bounded device-side wait gave up (no hang; context still usable) */
+#define APPFIS_GB_ENUMERIC 5     /* the computation stopped itself: a time step collapsed to zero or NaN */
 
 /* element types (reference Scatter/AllReduce support int, float, double: Communication.hpp:66-83) */
 #define APPFIS_GB_F32 0
 #define APPFIS_GB_F64 1
 #define APPFIS_GB_I32 2
+#define APPFIS_GB_F16 3          /* storage only (IEEE half); arithmetic stays FP32 */
 
 /* reduction operators, same order as the reference enum REDUCTION { MAX, MIN, SUM } (Appfis/Env.hpp:32) */
 #define APPFIS_GB_MAX 0
@@ -123,6 +125,97 @@ APPFIS_GB_API int appfis_gb_heat2d_sweep(const float* cur, float* next, int nx, 
 /* Whole run from host: field is the padded (nx+2)*(ny+2) dense array (ghost ring included), in
  * place.  stats (optional, 3 doubles): MAX, MIN, SUM of the interior at the end (reference seeds). */
 APPFIS_GB_API int appfis_gb_heat2d_job(float* field, int nx, int ny, int iters, float cx, float cy, double* stats);
+
+/* ----------------------------------------------------------------------------- Himeno */
+/* Replaces the per-iteration Execute3D(config, omega, a0..wrk1, p, wrk2) of the Himeno functor
+ * (Himeno/src/himeno_appfis.hpp:108-114,178-198) on a DUAL p grid with 12 SINGLE coefficient grids.
+ * coef: host array of 12 device pointers (a0 a1 a2 a3 b0 b1 b2 c0 c1 c2 bnd wrk1), each a padded
+ * (nx+2) x (ny+2) x (nz+2) FP32 field with row pitch `pitch`; p, wrk2: the two p buffers (zero
+ * ghost ring, as after the reference's Scatter).  The FP32 update follows the reference's
+ * summation order exactly (bit-identical to its CPU path).  dev_gosa (optional, `iters`
+ * doubles): gosa of every sweep = sum over the interior of ss^2 with ss as in :195, reduced in
+ * double inside the sweep (deterministic order); the reference computes no gosa. */
+APPFIS_GB_API int appfis_gb_himeno(const float* const* coef, float* p, float* wrk2, int nx, int ny, int nz, int pitch,
+                                   int iters, float omega, double* dev_gosa, int* cur_index, void* stream);
+/* Mixed-precision defect correction: FP16 storage of the correction e, the defect D and ten
+ * folded weights (26 B per point per sweep instead of 56), FP32 arithmetic, FP32 master p
+ * refreshed every `period` sweeps (the defect D = omega*ss(p) is then recomputed from the FP32
+ * coefficients).  Same iteration as appfis_gb_himeno in exact arithmetic; the difference is
+ * the FP16 rounding of the last period's correction.  p_work: a second FP32 field;
+ * half_work: 13 FP16 fields (13 * pitch*(ny+2)*(nz+2) halves).  gosa as above (from the FP16
+ * iterate, FP32 ss, double sum). */
+APPFIS_GB_API int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, void* half_work, int nx, int ny,
+                                         int nz, int pitch, int iters, int period, float omega, double* dev_gosa,
+                                         int* cur_index, void* stream);
+/* Whole run from host: coef_host = 12 dense padded fields back to back, p_host = dense padded p
+ * (in place).  form 0 = plain FP32, 1 = defect correction with `period`.  gosa_host: `iters`
+ * doubles or NULL. */
+APPFIS_GB_API int appfis_gb_himeno_job(const float* coef_host, float* p_host, int nx, int ny, int nz, int iters,
+                                       float omega, int form, int period, double* gosa_host);
+
+/* ----------------------------------------------------------------------------- radius-4 star (FDTD3d) */
+/* Replaces the per-step Execute3D(config, coeff, radius, cur, next) of the FDTD3d functor
+ * (FDTD3d/src/fdtd3d_appfis.hpp:84-87,129-143) with radius 4 on a DUAL grid with a ghost halo of
+ * width 4 (a, b: padded (nx+8) x (ny+8) x (nz+8), pitch >= nx+8, halo held at its values).
+ * mode 0: the reference form  v = c + sum_{a=1..4} ((x-a + x+a) + (y-a + y+a) + (z-a + z+a)),
+ *         v *= coeff  (same order; FP32 results bit-identical to the reference CPU path).
+ * mode 1: weighted form  v = w[0]*c + sum_a w[a]*((x-a + x+a) + (y-a + y+a) + (z-a + z+a)).
+ * dtype: APPFIS_GB_F32 or APPFIS_GB_F16 (storage).  tile_rows (2 or 4, 0 = 4) and zchunk (planes
+ * per CTA, 0 = 64) select the tile shape (see appfis_gb_star_r4_tune). */
+APPFIS_GB_API int appfis_gb_star_r4(void* a, void* b, int dtype, int nx, int ny, int nz, int pitch, int iters, int mode,
+                                    float coeff, const float* weights, int tile_rows, int zchunk, int* cur_index,
+                                    void* stream);
+
+/* ----------------------------------------------------------------------------- Triton flood model */
+/* Replaces the reference's Triton time loop (Triton/src/triton_appfis.hpp:316-386: CFL dt functor +
+ * Execute2DReduce(MIN) + host clamp, sqrt/RHS reset, X and Y Roe-type flux functors, update +
+ * Manning friction, HaloExchange, wet/dry fix) for a BATCH of independent domains of uneven
+ * sizes advanced in one persistent cooperative launch, each domain with its own dt, simulated
+ * time and step count, until every domain reaches t_end (or max_steps).  Point sources
+ * (:352-373) are not part of this entry point.
+ * A domain: padded (nx+2) x (ny+2) fields with row pitch `pitch`, element type `dtype`
+ * (APPFIS_GB_F32 or APPFIS_GB_F64): h/qx/qy[0] = state at t_start, h/qx/qy[1] = second buffers
+ * with the same ghost ring (0); dem with its ghost ring at the wall height (the reference uses
+ * 1e6); n2 = Manning n^2.  After the run the newest state of domain d is in buffer
+ * (steps[d] & 1), with the wet/dry fix of the last step applied. */
+typedef struct {
+    int nx, ny, pitch;
+    void* h[2];
+    void* qx[2];
+    void* qy[2];
+    const void* dem;
+    const void* n2;
+} appfis_gb_flood_domain;
+
+typedef struct {
+    double dx;             /* cell size (m) */
+    double courant;        /* CFL number cn */
+    double hextra;         /* wet threshold (m) */
+    double t_end;          /* simulated end time (s) */
+    double print_interval; /* dt is clamped so that the simulated time lands on multiples of it */
+    double time_step;      /* dt used while no cell is wet */
+    double t_start;        /* initial simulated time */
+    int max_steps;         /* 0 = no limit; > 0 also enables the dt log */
+} appfis_gb_flood_params;
+
+#define APPFIS_GB_FLOOD_MAX_DOMAINS 64
+
+/* Device entry: dev_dtlog (optional, ndom*max_steps doubles, needs max_steps > 0): dt of every
+ * step; dev_steps / dev_simtime (optional, ndom each): steps taken and final time; dev_status
+ * (optional int): APPFIS_GB_OK, APPFIS_GB_ETIMEOUT if a bounded grid-wide wait gave up, or
+ * APPFIS_GB_ENUMERIC if a domain's time step collapsed to zero or NaN (the run stops).  With
+ * max_steps = 0 each domain is capped at 1,000,000 steps. */
+APPFIS_GB_API int appfis_gb_flood_run(const appfis_gb_flood_domain* doms, int ndom, int dtype,
+                                      const appfis_gb_flood_params* prm, double* dev_dtlog, int* dev_steps,
+                                      double* dev_simtime, int* dev_status, void* stream);
+/* Host-buffer job: per domain nx*ny FP64 interiors dem[d], h[d] (in/out), qx[d]/qy[d] (in/out,
+ * may be NULL = zero initial momentum, not returned); computed in `dtype`.  steps_out (ndom),
+ * mass_out (2*ndom: sum of h over the interior before and after, FP64), dtlog_host (ndom*max_steps)
+ * are optional. */
+APPFIS_GB_API int appfis_gb_flood_job(int ndom, const int* nx, const int* ny, const double* const* dem, double* const* h,
+                                      double* const* qx, double* const* qy, double manning,
+                                      const appfis_gb_flood_params* prm, int dtype, int* steps_out, double* mass_out,
+                                      double* dtlog_host);
 
 #ifdef __cplusplus
 }

@@ -177,6 +177,9 @@ struct Phys {
     static constexpr T g = T(9.81);          // G      (:53)
     static constexpr T sqrtg = T(3.132091953);  // SQRTG  (:54)
     static constexpr T eps = T(1e-12);       // EPS12  (:55)
+    // "this cell is dry" threshold on depths: EPS12 in double; in float a depth that should be
+    // exactly 0 keeps a rounding residual of ~1e-8 m, so the float form uses 1e-6 m.
+    static constexpr T dry = sizeof(T) == sizeof(double) ? T(1e-12) : T(1e-6);
 };
 
 // One face; returns false when both cells are dry (the reference then writes nothing).
@@ -184,7 +187,7 @@ template <class T>
 bool roe_face(T h1, T h2, T qx1, T qy1, T qx2, T qy2, T z1, T z2, T sqh1, T sqh2, T nx, T ny, T dx, T dt,
               T hextra, T d1[3], T d2[3])
 {
-    const T G = Phys<T>::g, SG = Phys<T>::sqrtg, E = Phys<T>::eps;
+    const T G = Phys<T>::g, SG = Phys<T>::sqrtg, E = Phys<T>::eps, ED = Phys<T>::dry;
     if (!(h1 > T(0) || h2 > T(0))) return false;
     T u1 = 0, v1 = 0, u2 = 0, v2 = 0;
     if (h1 >= hextra) { u1 = qx1 / h1; v1 = qy1 / h1; }
@@ -242,9 +245,9 @@ bool roe_face(T h1, T h2, T qx1, T qy1, T qx2, T qy2, T z1, T z2, T sqh1, T sqh2
     for (int i = 0; i < 3; i++) d1[i] = d2[i] = 0;
     l1 = hp - be[0] / lam[0];
     l2 = hp + be[2] / lam[2];
-    if (l2 < -E && h2 < E)
+    if (l2 < -ED && h2 < ED)
         d1[0] += (lam[0] * al[0] - be[0]) + (lam[2] * al[2] - be[2]);
-    else if (l1 < -E && h1 < E)
+    else if (l1 < -ED && h1 < ED)
         d2[0] += (lam[0] * al[0] - be[0]) + (lam[2] * al[2] - be[2]);
     else
         for (int i = 0; i < 3; i++)
@@ -376,8 +379,14 @@ double triton_step(TritonState<T>& s, T dx, T cn, T hextra, double time_step, do
                 if (nn > E && hn >= hextra && modM > E)
                 {
                     T tt = tdt * G * nn * modM / (hn * hn * std::cbrt(hn));
-                    qxij = T(-0.5) * (mx - mx * std::sqrt(T(1) + T(4) * tt)) / tt;
-                    qyij = T(-0.5) * (my - my * std::sqrt(T(1) + T(4) * tt)) / tt;
+                    if (sizeof(T) == sizeof(double)) {  // the reference's form
+                        qxij = T(-0.5) * (mx - mx * std::sqrt(T(1) + T(4) * tt)) / tt;
+                        qyij = T(-0.5) * (my - my * std::sqrt(T(1) + T(4) * tt)) / tt;
+                    } else {  // FP32: the same quantity without the cancellation of 1 - sqrt(1 + 4 tt)
+                        const T den = T(1) + std::sqrt(T(1) + T(4) * tt);
+                        qxij = T(2) * mx / den;
+                        qyij = T(2) * my / den;
+                    }
                 }
                 else { qxij = mx; qyij = my; }
             }
@@ -392,10 +401,11 @@ double triton_step(TritonState<T>& s, T dx, T cn, T hextra, double time_step, do
         {
             size_t c = at2(i, j, px);
             T hij = h[c], zij = dem[c];
+            const T ED = Phys<T>::dry;
             if (hij > hextra)
             {
-                if (((hij + zij < dem[c + 1]) && (h[c + 1] < E)) || ((hij + zij < dem[c - 1]) && (h[c - 1] < E))) qx[c] = 0;
-                if (((hij + zij < dem[c - px]) && (h[c - px] < E)) || ((hij + zij < dem[c + px]) && (h[c + px] < E))) qy[c] = 0;
+                if (((hij + zij < dem[c + 1]) && (h[c + 1] < ED)) || ((hij + zij < dem[c - 1]) && (h[c - 1] < ED))) qx[c] = 0;
+                if (((hij + zij < dem[c - px]) && (h[c - px] < ED)) || ((hij + zij < dem[c + px]) && (h[c + px] < ED))) qy[c] = 0;
             }
         }
     simtime += dt;

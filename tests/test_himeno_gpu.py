@@ -1,0 +1,88 @@
+"""Himeno kernels vs the oracle: the FP32 plain form bit-identical to the reference's CPU path
+(golden fixture + random coefficient fields), gosa within 1e-12 of the oracle's double sum;
+the FP16 defect-correction form within its stated error of the FP64 oracle."""
+import ctypes
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from appfis_gb300 import workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def job(gb, coef, p, iters, form=0, period=20, omega=0.8):
+    nz, ny, nx = p.shape[0] - 2, p.shape[1] - 2, p.shape[2] - 2
+    out = np.ascontiguousarray(p, dtype=np.float32).copy()
+    c = np.ascontiguousarray(coef, dtype=np.float32)
+    gosa = np.zeros(max(iters, 1), dtype=np.float64)
+    gb.call("appfis_gb_himeno_job", c.ctypes.data, out.ctypes.data, nx, ny, nz, iters, omega, form, period,
+            gosa.ctypes.data)
+    return out, gosa[:iters]
+
+
+@pytest.mark.parametrize("f", sorted(glob.glob(os.path.join(GOLD, "himeno_*.npz"))), ids=os.path.basename)
+def test_golden_bit_exact(gb, torch_cuda, f):
+    g = np.load(f)
+    out, gosa = job(gb, g["coef"], g["p"], int(g["iters"]))
+    assert np.array_equal(out, g["out"])
+    np.testing.assert_allclose(gosa, g["gosa"], rtol=1e-12)
+
+
+@pytest.mark.parametrize("nx,ny,nz,iters", [(1, 1, 1, 3), (33, 5, 40, 6), (70, 41, 9, 4), (257, 9, 65, 3)])
+def test_random_vs_oracle(gb, torch_cuda, nx, ny, nz, iters):
+    coef = W.himeno_coef(nx, ny, nz, seed=nx + ny + nz)
+    p = W.himeno_p(nx, ny, nz)
+    p[1:-1, 1:-1, 1:-1] += W.uniform(3, nx * ny * nz).reshape(nz, ny, nx).astype(np.float32)
+    out, gosa = job(gb, coef, p, iters)
+    ref, rgosa = O.himeno(coef, p, iters, 0.8)
+    assert np.array_equal(out, ref)
+    np.testing.assert_allclose(gosa, rgosa, rtol=1e-12)
+
+
+def test_device_entry_two_buffers(gb, torch_cuda):
+    torch = torch_cuda
+    nx, ny, nz, iters = 40, 30, 20, 5
+    coef = W.himeno_coef(nx, ny, nz)
+    p = W.himeno_p(nx, ny, nz)
+    dc = torch.from_numpy(coef).cuda()
+    ptrs = (ctypes.c_void_p * 12)(*[dc[k].data_ptr() for k in range(12)])
+    pitch = 64  # a padded pitch different from nx+2
+    hp = np.zeros((nz + 2, ny + 2, pitch), dtype=np.float32)
+    hp[:, :, : nx + 2] = p
+    hc = np.zeros((12, nz + 2, ny + 2, pitch), dtype=np.float32)
+    hc[..., : nx + 2] = coef
+    dc = torch.from_numpy(hc).cuda()
+    ptrs = (ctypes.c_void_p * 12)(*[dc[k].data_ptr() for k in range(12)])
+    a = torch.from_numpy(hp).cuda()
+    b = a.clone()
+    g = torch.zeros(iters, dtype=torch.float64, device="cuda")
+    ci = ctypes.c_int(-1)
+    gb.call("appfis_gb_himeno", ptrs, a.data_ptr(), b.data_ptr(), nx, ny, nz, pitch, iters, 0.8, g.data_ptr(),
+            ctypes.byref(ci), None)
+    out = (a if ci.value == 0 else b).cpu().numpy()[:, :, : nx + 2]
+    ref, rg = O.himeno(coef, p, iters, 0.8)
+    assert np.array_equal(out, ref)
+    np.testing.assert_allclose(g.cpu().numpy(), rg, rtol=1e-12)
+
+
+def test_mixed_defect_correction_error(gb, torch_cuda):
+    """FP16-storage defect correction vs the FP64 oracle on the benchmark's coefficient set:
+    p within 2e-4 absolute (p is O(1)), gosa within 1% relative, per sweep."""
+    nx, ny, nz, iters = 65, 65, 129, 60
+    coef32 = W.himeno_coef(nx, ny, nz)
+    p32 = W.himeno_p(nx, ny, nz)
+    p64, g64 = O.himeno(W.himeno_coef(nx, ny, nz, dtype=np.float64), W.himeno_p(nx, ny, nz, dtype=np.float64), iters, 0.8,
+                        dtype=np.float64)
+    plain, gp = job(gb, coef32, p32, iters, form=0)
+    mixed, gm = job(gb, coef32, p32, iters, form=1, period=20)
+    err_plain = np.abs(plain - p64).max()
+    err_mixed = np.abs(mixed - p64).max()
+    assert err_plain < 1e-5
+    assert err_mixed < 2e-4, err_mixed
+    np.testing.assert_allclose(gm, g64, rtol=1e-2)
+    np.testing.assert_allclose(gp, g64, rtol=1e-4)

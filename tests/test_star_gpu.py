@@ -1,0 +1,70 @@
+"""Radius-4 star (FDTD3d) kernels vs the oracle: the reference form bit-identical (golden
+fixture from the reference, odd sizes), the weighted form within FP32 rounding of the FP32
+oracle, the FP16-storage form within its stated error of the FP64 oracle."""
+import ctypes
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from appfis_gb300 import workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def run(gb, torch, padded, iters, mode, coeff=0.1, weights=None, dtype="f32", pitch=None, ry=0, kz=0):
+    nz, ny, nx = padded.shape[0] - 8, padded.shape[1] - 8, padded.shape[2] - 8
+    pitch = pitch or nx + 8
+    host = np.zeros(padded.shape[:2] + (pitch,), dtype=np.float32)
+    host[..., : nx + 8] = padded
+    tdt = torch.float32 if dtype == "f32" else torch.float16
+    a = torch.from_numpy(host).cuda().to(tdt)
+    b = a.clone()
+    w = None if weights is None else (ctypes.c_float * 5)(*weights)
+    ci = ctypes.c_int(-1)
+    gb.call("appfis_gb_star_r4", a.data_ptr(), b.data_ptr(), 0 if dtype == "f32" else 3, nx, ny, nz, pitch, iters, mode,
+            coeff, w, ry, kz, ctypes.byref(ci), None)
+    out = (a if ci.value == 0 else b).float().cpu().numpy()
+    return out[..., : nx + 8]
+
+
+@pytest.mark.parametrize("f", sorted(glob.glob(os.path.join(GOLD, "fdtd_*.npz"))), ids=os.path.basename)
+def test_golden_reference_form(gb, torch_cuda, f):
+    g = np.load(f)
+    out = run(gb, torch_cuda, g["padded"], int(g["iters"]), 0, float(g["coeff"]))
+    assert np.array_equal(out, g["out"])
+
+
+@pytest.mark.parametrize("nx,ny,nz,iters,ry,kz,pitch", [(1, 1, 1, 2, 0, 0, None), (37, 29, 11, 3, 4, 0, None),
+                                                        (64, 70, 33, 2, 2, 16, 80), (33, 17, 130, 2, 4, 64, None),
+                                                        (100, 3, 5, 4, 2, 3, 112)])
+def test_reference_form_vs_oracle(gb, torch_cuda, nx, ny, nz, iters, ry, kz, pitch):
+    f = W.fdtd_padded(nx, ny, nz, nx * ny + nz)
+    out = run(gb, torch_cuda, f, iters, 0, 0.1, pitch=pitch, ry=ry, kz=kz)
+    assert np.array_equal(out, O.star_r4(f, iters, coeff=0.1))
+
+
+def test_weighted_form_vs_oracle(gb, torch_cuda):
+    w = W.fdtd_weights()
+    f = W.fdtd_padded(48, 40, 36, 5)
+    out = run(gb, torch_cuda, f, 10, 1, weights=w)
+    ref32 = O.star_r4(f, 10, weights=w)
+    ref64 = O.star_r4(f.astype(np.float64), 10, weights=w, dtype=np.float64)
+    assert np.abs(out - ref32).max() < 1e-5
+    assert np.abs(out - ref64).max() < 1e-5
+    assert np.all(out[:4] == 0) and np.all(out[..., :4] == 0)  # halo untouched
+
+
+def test_fp16_storage_error(gb, torch_cuda):
+    """FP16 storage, FP32 arithmetic, 50 steps of u <- u + nu*L8(u): max error vs FP64 < 2e-3
+    (inputs in [-1, 1]); the FP32 form stays within 1e-5."""
+    w = W.fdtd_weights()
+    f = W.fdtd_padded(64, 64, 64, 9)
+    ref64 = O.star_r4(f.astype(np.float64), 50, weights=w, dtype=np.float64)
+    o32 = run(gb, torch_cuda, f, 50, 1, weights=w)
+    o16 = run(gb, torch_cuda, f, 50, 1, weights=w, dtype="f16")
+    assert np.abs(o32 - ref64).max() < 1e-5
+    assert np.abs(o16 - ref64).max() < 2e-3
