@@ -1,0 +1,249 @@
+/*
+ * Runtime.hpp — InitializeExecution / FinalizeExecution / Execute{1,2,3}D / Execute*DReduce /
+ * HaloExchange of the GB300 APPFIS engine (reference: Appfis/Runtime.hpp:23-255 dispatch,
+ * Appfis/Runtime_CUDA.hpp:231-740 GPU path).
+ *
+ * Execute*D(config, args...) launches one generic kernel over the Config box that calls the
+ * user's Stencil(i[, j[, k]], args...) per point, exactly like the reference's Kernel{1,2,3}D
+ * (Runtime_CUDA.hpp:1201-1246), with three differences:
+ *   - every Array<T>* argument travels by value (pointer + dims) and is rebuilt in registers,
+ *     so Get/Set do no dependent load of a dims pointer;
+ *   - blocks are 32 wide in x (coalesced rows) for every dimensionality;
+ *   - after the sweep, the grids named by GridsToUpdate get their periodic ghosts refreshed on
+ *     the device (no pack / host copy / MPI round trip) and are swapped; with one rank and no
+ *     periodic axis there is nothing to exchange, as in the reference.
+ * Reductions run on the device in one deterministic launch (appfis_gb_reduce) and return the
+ * value to the host like the reference's Execute*DReduceGPU (Runtime_CUDA.hpp:554-740), seeds
+ * included (MAX starts from numeric_limits<T>::min()); the input grid is never overwritten.
+ * The reference's GPU 1-D executor swaps the updated grids twice (Runtime_CUDA.hpp:295-296), a
+ * net no-op; here every executor swaps once, like the reference's CPU path (Runtime.hpp:318-319).
+ */
+#ifndef APPFIS_GB_RUNTIME_HPP
+#define APPFIS_GB_RUNTIME_HPP
+
+#include <cstdlib>
+#include <iostream>
+#include <type_traits>
+
+#include "Config.hpp"
+#include "Grid.hpp"
+
+namespace APPFIS
+{
+
+	namespace detail
+	{
+		inline int gb_launch_status()
+		{
+			const cudaError_t e = cudaGetLastError();
+			if (e == cudaSuccess) return APPFIS_GB_OK;
+			std::cerr << "APPFIS engine: " << cudaGetErrorString(e) << std::endl;
+			return APPFIS_GB_ECUDA;
+		}
+
+		// Host -> kernel argument conversion: Array<U>* becomes a by-value view of device memory.
+		template<class A>
+		struct KArg
+		{
+			typedef A type;
+			static A to(A a) { return a; }
+		};
+
+		template<class U>
+		struct KArg<Array<U>*>
+		{
+			typedef ArrayArg<U> type;
+			static ArrayArg<U> to(Array<U>* a)
+			{
+				cudaPointerAttributes attr;
+				if (a == nullptr || a->GetData() == nullptr || cudaPointerGetAttributes(&attr, a->GetData()) != cudaSuccess ||
+					attr.type != cudaMemoryTypeDevice)
+				{
+					cudaGetLastError();
+					std::cerr << "APPFIS engine: an Array passed to Execute*D is not on the device; pass grid.GetSubGrid() "
+						"after InitializeExecution(grid)." << std::endl;
+					std::exit(EXIT_FAILURE);
+				}
+				return a->Arg();
+			}
+		};
+
+		// Kernel side: scalars pass through, array views are rebuilt as local Array objects.
+		template<class A>
+		struct Holder
+		{
+			A v;
+			__device__ explicit Holder(const A& a) : v(a) {}
+			__device__ A get() const { return v; }
+		};
+
+		template<class U>
+		struct Holder<ArrayArg<U> >
+		{
+			Array<U> a;
+			__device__ explicit Holder(const ArrayArg<U>& g) : a(g) {}
+			__device__ Array<U>* get() { return &a; }
+		};
+
+		template<class... A>
+		__global__ void Functor1D(int x0, int x1, A... args)
+		{
+			const int i = x0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+			if (i < x1) STENCIL(i, Holder<A>(args).get()...);
+		}
+
+		template<class... A>
+		__global__ void Functor2D(int x0, int x1, int y0, int y1, A... args)
+		{
+			const int i = x0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+			const int j = y0 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+			if (i < x1 && j < y1) STENCIL(i, j, Holder<A>(args).get()...);
+		}
+
+		template<class... A>
+		__global__ void Functor3D(int x0, int x1, int y0, int y1, int z0, int z1, A... args)
+		{
+			const int i = x0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+			const int j = y0 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+			const int k = z0 + (int)(blockIdx.z * blockDim.z + threadIdx.z);
+			if (i < x1 && j < y1 && k < z1) STENCIL(i, j, k, Holder<A>(args).get()...);
+		}
+
+		inline unsigned Blocks(int n, int b) { return (unsigned)((n + b - 1) / b); }
+
+		template<class T>
+		void RefreshGhosts(Grid<T>* g, bool next)
+		{
+			if (GetGhostLayer() <= 0 || !IsPeriodic() || g->GetGridType() == FLAT) return;
+			Array<T>* a = next ? g->GetSubGridNextCPU() : g->GetSubGridCPU();
+			const int d[3] = { a->GetDim(0), a->GetDim(1), a->GetDim(2) };
+			Check(appfis_gb_ghost_periodic(next ? g->DeviceNext() : g->DeviceCurrent(), (int)sizeof(T), a->GetDimCount(), d,
+				GetGhostLayer(), GetCudaStream()), "periodic ghost refresh");
+		}
+
+		// After a sweep: refresh the updated grids' next buffers, then swap them in.
+		template<class T>
+		void AfterSweep(Config<T>& config)
+		{
+			Check(gb_launch_status(), "stencil kernel launch");
+			for (size_t n = 0; n < config.updatedGrids.size(); n++) RefreshGhosts(config.updatedGrids[n], true);
+			for (size_t n = 0; n < config.updatedGrids.size(); n++) config.updatedGrids[n]->Swap();
+		}
+
+		template<class T> struct DType;
+		template<> struct DType<float> { static const int code = APPFIS_GB_F32; };
+		template<> struct DType<double> { static const int code = APPFIS_GB_F64; };
+		template<> struct DType<int> { static const int code = APPFIS_GB_I32; };
+	}
+
+	template<typename T>
+	void InitializeExecution(Grid<T>& grid)
+	{
+		ExecutionFlag() = true;
+		grid.Upload(GetCudaStream());
+		if (grid.GetGridType() != FLAT)
+		{
+			detail::RefreshGhosts(&grid, false);  // ExchangeInitial on both buffers (Runtime.hpp:128-136)
+			if (grid.GetGridType() == DUAL) detail::RefreshGhosts(&grid, true);
+		}
+	}
+
+	template<typename T, typename... TArgs>
+	void InitializeExecution(Grid<T>& grid, TArgs&&... args)
+	{
+		InitializeExecution(grid);
+		InitializeExecution(args...);
+	}
+
+	template<typename T>
+	void FinalizeExecution(Grid<T>& grid)
+	{
+		ExecutionFlag() = false;
+		grid.DownloadCurrent(GetCudaStream());
+	}
+
+	template<typename T, typename... TArgs>
+	void FinalizeExecution(Grid<T>& grid, TArgs&&... args)
+	{
+		FinalizeExecution(grid);
+		FinalizeExecution(args...);
+	}
+
+	template<typename T, typename... TArgs>
+	void Execute1D(Config<T>& config, TArgs... args)
+	{
+		const int x0 = config.GetStartX(), x1 = config.GetEndX();
+		if (x1 > x0)
+			detail::Functor1D<typename detail::KArg<TArgs>::type...><<<detail::Blocks(x1 - x0, 256), 256, 0, GetCudaStream()>>>(
+				x0, x1, detail::KArg<TArgs>::to(args)...);
+		detail::AfterSweep(config);
+	}
+
+	template<typename T, typename... TArgs>
+	void Execute2D(Config<T>& config, TArgs... args)
+	{
+		const int x0 = config.GetStartX(), x1 = config.GetEndX(), y0 = config.GetStartY(), y1 = config.GetEndY();
+		if (x1 > x0 && y1 > y0)
+		{
+			dim3 blk(32, 8), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 8));
+			detail::Functor2D<typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
+				x0, x1, y0, y1, detail::KArg<TArgs>::to(args)...);
+		}
+		detail::AfterSweep(config);
+	}
+
+	template<typename T, typename... TArgs>
+	void Execute3D(Config<T>& config, TArgs... args)
+	{
+		const int x0 = config.GetStartX(), x1 = config.GetEndX(), y0 = config.GetStartY(), y1 = config.GetEndY();
+		const int z0 = config.GetStartZ(), z1 = config.GetEndZ();
+		if (x1 > x0 && y1 > y0 && z1 > z0)
+		{
+			dim3 blk(32, 4, 2), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 4), detail::Blocks(z1 - z0, 2));
+			detail::Functor3D<typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
+				x0, x1, y0, y1, z0, z1, detail::KArg<TArgs>::to(args)...);
+		}
+		detail::AfterSweep(config);
+	}
+
+	namespace detail
+	{
+		template<typename T>
+		void Reduce(Config<T>& config, T& var, REDUCTION rType, Grid<T>& grid, int nDim)
+		{
+			if (!grid.OnDevice())
+			{
+				std::cerr << "APPFIS engine: Execute*DReduce needs InitializeExecution(grid) first." << std::endl;
+				std::exit(EXIT_FAILURE);
+			}
+			Array<T>* a = grid.GetSubGridCPU();
+			const int box[6] = { config.GetStartX(), config.GetEndX(),
+				nDim > 1 ? config.GetStartY() : 0, nDim > 1 ? config.GetEndY() : 1,
+				nDim > 2 ? config.GetStartZ() : 0, nDim > 2 ? config.GetEndZ() : 1 };
+			double r = 0.0;
+			Check(appfis_gb_reduce_host(grid.DeviceCurrent(), DType<T>::code, a->GetDim(0), a->GetDimCount() > 1 ? a->GetDim(1) : 1,
+				box, (int)rType, &r, GetCudaStream()), "reduction");
+			var = (T)r;
+		}
+	}
+
+	template<typename T>
+	void Execute1DReduce(Config<T>& config, T& var, REDUCTION rType, Grid<T>& grid) { detail::Reduce(config, var, rType, grid, 1); }
+
+	template<typename T>
+	void Execute2DReduce(Config<T>& config, T& var, REDUCTION rType, Grid<T>& grid) { detail::Reduce(config, var, rType, grid, 2); }
+
+	template<typename T>
+	void Execute3DReduce(Config<T>& config, T& var, REDUCTION rType, Grid<T>& grid) { detail::Reduce(config, var, rType, grid, 3); }
+
+	// Refresh the ghosts of the grid's next buffer and swap it in (Runtime.hpp:173-189).
+	template<typename T>
+	void HaloExchange(Grid<T>* grid)
+	{
+		detail::RefreshGhosts(grid, true);
+		grid->Swap();
+	}
+
+}
+
+#endif

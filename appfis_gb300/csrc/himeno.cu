@@ -12,12 +12,14 @@
 //
 // Defect-correction form (FP16 storage, FP32 arithmetic).  With p = P + e (P an FP32 master
 // frozen between corrections) the Jacobi update p' = p + w*bnd*(a3*(N p + wrk1) - p) becomes
-//     e' = Wc*e + sum_n Wn*(e neighbour terms) + D,   Wc = 1 - w*bnd,  Wn = w*bnd*a3*coef_n,
-//     D  = w*ss(P)   (the FP32 defect of the master),
-// an exact rewrite.  Inner sweeps read e, D and the 10 folded weights in FP16 (26 B per point
-// instead of 56).  Every `period` sweeps a correction pass folds e into P, recomputes D from
-// the FP32 coefficients and restarts e at 0, which bounds the FP16 error to the last period's
-// correction.  The sweep's own ss is (e' - e)/w (FP32, before rounding e').
+//     e' = e + w*bnd*(a3*N e - e) + D,    D = w*ss(P)   (the FP32 defect of the master),
+// an exact rewrite (N = the 18 neighbour terms of s0 without wrk1).  Inner sweeps read e, D and
+// the ten neighbour/boundary coefficient fields (a0 a1 a2 b0 b1 b2 c0 c1 c2 bnd) in FP16 and the
+// diagonal scale a3 in FP32 (it multiplies the whole neighbour sum, so its rounding would bias
+// every point coherently): 30 B per point per sweep instead of 56.  Every `period` sweeps a
+// correction pass folds e into P, recomputes D from the FP32 coefficients and restarts e at 0,
+// which bounds the FP16 error to the last period's correction.  The sweep's own ss is
+// (e' - e)/w (FP32, before rounding e').
 #include <cuda_fp16.h>
 
 #include "gb_common.cuh"
@@ -27,8 +29,9 @@ namespace {
 struct Coef12 {
     const float* c[12];  // a0 a1 a2 a3 b0 b1 b2 c0 c1 c2 bnd wrk1
 };
-struct W10 {
-    const __half* w[10];  // xp yp zp b0 b1 b2 xm ym zm centre
+struct H10 {
+    const __half* c[10];  // a0 a1 a2 b0 b1 b2 c0 c1 c2 bnd in FP16
+    const float* a3;      // FP32
 };
 
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
@@ -123,21 +126,17 @@ __global__ void __launch_bounds__(BX* BY) himeno_sweep(Coef12 cf, const float* _
 }
 
 // ---------------------------------------------------------------- defect-correction form
-// Folded FP16 weights from the FP32 coefficients (over the interior; ghosts stay 0).
-__global__ void himeno_fold_weights(Coef12 cf, __half* __restrict__ w, size_t field, int nx, int ny, int nz, int px,
-                                    int py, float omega)
+// FP16 copies of the ten neighbour / boundary coefficient fields (over the interior).
+__global__ void himeno_half_coef(Coef12 cf, __half* __restrict__ w, size_t field, int nx, int ny, int nz, int px, int py)
 {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y;
     const int k = 1 + blockIdx.z;
     if (i > nx) return;
     const size_t c = ((size_t)k * py + j) * px + i;
-    const float wb = omega * cf.c[10][c];
-    const float s = wb * cf.c[3][c];
-    const int map[9] = {0, 1, 2, 4, 5, 6, 7, 8, 9};  // xp yp zp b0 b1 b2 xm ym zm
+    const int map[10] = {0, 1, 2, 4, 5, 6, 7, 8, 9, 10};  // a0 a1 a2 b0 b1 b2 c0 c1 c2 bnd
 #pragma unroll
-    for (int n = 0; n < 9; n++) w[n * field + c] = __float2half_rn(s * cf.c[map[n]][c]);
-    w[9 * field + c] = __float2half_rn(1.0f - wb);
+    for (int n = 0; n < 10; n++) w[n * field + c] = __float2half_rn(cf.c[map[n]][c]);
 }
 
 // Correction pass: P' = P + e, D = omega*ss(P'), e_next = 0.  Reads P and e at neighbours.
@@ -171,9 +170,9 @@ __global__ void __launch_bounds__(BX* BY) himeno_correct(Coef12 cf, const float*
 }
 
 template <int BX, int BY>
-__global__ void __launch_bounds__(BX* BY) himeno_inner(W10 wf, const __half* __restrict__ e, const __half* __restrict__ D,
+__global__ void __launch_bounds__(BX* BY) himeno_inner(H10 hf, const __half* __restrict__ e, const __half* __restrict__ D,
                                                         __half* __restrict__ en, int nx, int ny, int nz, int px, int py,
-                                                        int kz, float inv_omega, double* __restrict__ partials,
+                                                        int kz, float omega, float inv_omega, double* __restrict__ partials,
                                                         unsigned* __restrict__ ticket, double* __restrict__ gosa)
 {
     const int i = 1 + blockIdx.x * BX + threadIdx.x;
@@ -189,15 +188,15 @@ __global__ void __launch_bounds__(BX* BY) himeno_inner(W10 wf, const __half* __r
 #define EF(di, dj, dk)                                            \
     ((di) == 0 && (dj) == 0 ? ((dk) < 0 ? em : ((dk) > 0 ? ep : e0)) \
                             : __half2float(e[c + (ptrdiff_t)(di) + (ptrdiff_t)(dj) * px + (ptrdiff_t)(dk) * (ptrdiff_t)plane]))
-#define WF(n) __half2float(wf.w[n][c])
-            float v = WF(9) * e0 + __half2float(D[c]);
-            v += WF(0) * EF(1, 0, 0) + WF(1) * EF(0, 1, 0) + WF(2) * EF(0, 0, 1);
-            v += WF(3) * ((EF(1, 1, 0) - EF(1, -1, 0)) - (EF(-1, 1, 0) - EF(-1, -1, 0)));
-            v += WF(4) * ((EF(0, 1, 1) - EF(0, -1, 1)) - (EF(0, 1, -1) - EF(0, -1, -1)));
-            v += WF(5) * ((EF(1, 0, 1) - EF(-1, 0, 1)) - (EF(1, 0, -1) - EF(-1, 0, -1)));
-            v += WF(6) * EF(-1, 0, 0) + WF(7) * EF(0, -1, 0) + WF(8) * EF(0, 0, -1);
+#define CF(n) __half2float(hf.c[n][c])
+            float ne = CF(0) * EF(1, 0, 0) + CF(1) * EF(0, 1, 0) + CF(2) * EF(0, 0, 1);
+            ne += CF(3) * ((EF(1, 1, 0) - EF(1, -1, 0)) - (EF(-1, 1, 0) - EF(-1, -1, 0)));
+            ne += CF(4) * ((EF(0, 1, 1) - EF(0, -1, 1)) - (EF(0, 1, -1) - EF(0, -1, -1)));
+            ne += CF(5) * ((EF(1, 0, 1) - EF(-1, 0, 1)) - (EF(1, 0, -1) - EF(-1, 0, -1)));
+            ne += CF(6) * EF(-1, 0, 0) + CF(7) * EF(0, -1, 0) + CF(8) * EF(0, 0, -1);
+            const float v = e0 + omega * CF(9) * (__ldg(hf.a3 + c) * ne - e0) + __half2float(D[c]);
 #undef EF
-#undef WF
+#undef CF
             en[c] = __float2half_rn(v);
             const float ss = (v - e0) * inv_omega;
             g += (double)ss * (double)ss;
@@ -272,16 +271,17 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     cudaStream_t st = gb::as_stream(stream);
     const size_t field = (size_t)pitch * (ny + 2) * (nz + 2);
     __half* hw = reinterpret_cast<__half*>(half_work);
-    __half* W = hw;                   // 10 fields
+    __half* Hc = hw;                  // 10 FP16 coefficient fields
     __half* E[2] = {hw + 10 * field, hw + 11 * field};
     __half* Dd = hw + 12 * field;
     Coef12 cf;
     for (int n = 0; n < 12; n++) cf.c[n] = coef[n];
-    W10 wf;
-    for (int n = 0; n < 10; n++) wf.w[n] = W + n * field;
+    H10 hf;
+    for (int n = 0; n < 10; n++) hf.c[n] = Hc + n * field;
+    hf.a3 = coef[3];
     GB_CUDA(cudaMemsetAsync(hw, 0, sizeof(__half) * 13 * field, st));
     GB_CUDA(cudaMemsetAsync(p_work, 0, sizeof(float) * field, st));
-    himeno_fold_weights<<<dim3(gb::ceil_div(nx, 128), ny, nz), 128, 0, st>>>(cf, W, field, nx, ny, nz, pitch, ny + 2, omega);
+    himeno_half_coef<<<dim3(gb::ceil_div(nx, 128), ny, nz), 128, 0, st>>>(cf, Hc, field, nx, ny, nz, pitch, ny + 2);
     dim3 blk(HBX, HBY), grd(gb::ceil_div(nx, HBX), gb::ceil_div(ny, HBY), gb::ceil_div(nz, HKZ));
     double* partials = nullptr;
     unsigned* ticket = nullptr;
@@ -294,7 +294,7 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     ec = 1 - ec;
     const float inv_omega = 1.0f / omega;
     for (int it = 0; it < iters; it++) {
-        himeno_inner<HBX, HBY><<<grd, blk, 0, st>>>(wf, E[ec], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2, HKZ, inv_omega,
+        himeno_inner<HBX, HBY><<<grd, blk, 0, st>>>(hf, E[ec], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2, HKZ, omega, inv_omega,
                                                     partials, ticket, dev_gosa ? dev_gosa + it : nullptr);
         ec = 1 - ec;
         if ((it + 1) % period == 0 || it + 1 == iters) {

@@ -19,7 +19,7 @@ namespace {
 
 constexpr uint32_t FULL = 0xffffffffu;
 constexpr uint32_t LSB = 0x01010101u;  // bit 0 of each byte
-constexpr int LIFE_ROWS = 64;           // rows per warp task
+constexpr int LIFE_ROWS = 32;           // rows per warp task
 
 // ------------------------------------------------------------------------------ rule logic
 // Per byte lane (u8 form): cnt in 0..8 in each byte, c/o in {0,1} per byte.
@@ -67,66 +67,92 @@ __global__ void life_u8_generic(const uint8_t* __restrict__ cur, uint8_t* __rest
 }
 
 // ------------------------------------------------------------------------------ u8 SWAR form
+struct RawU8 {    // one row's loads for this lane, before the lane-boundary exchange
+    uint4 v;      // the 16 cells of this lane
+    uint32_t lw;  // lane 0: cell x0-1 in the top byte
+    uint32_t rw;  // last active lane: cell x0+16 in the low byte
+};
 struct RowU8 {
     uint32_t w[4];   // the 16 cells of this lane
     uint32_t s3[4];  // per byte: left + self + right
 };
 
-__device__ __forceinline__ void load_row_u8(const uint8_t* __restrict__ cur, int nx, int row, int x0, bool active,
-                                            int lane, RowU8& r)
+__device__ __forceinline__ RawU8 load_raw_u8(const uint8_t* __restrict__ cur, int nx, int row, int x0, bool active, int lane)
 {
     const uint8_t* p = cur + (size_t)row * nx;
-    uint4 v = active ? __ldg(reinterpret_cast<const uint4*>(p + x0)) : make_uint4(0, 0, 0, 0);
-    uint32_t lw = __shfl_up_sync(FULL, v.w, 1);
-    uint32_t rw = __shfl_down_sync(FULL, v.x, 1);
-    if (lane == 0) lw = (uint32_t)__ldg(p + (x0 == 0 ? nx - 1 : x0 - 1)) << 24;
-    if (active && (lane == 31 || x0 + 16 >= nx)) rw = __ldg(p + (x0 + 16 >= nx ? 0 : x0 + 16));
-    r.w[0] = v.x;
-    r.w[1] = v.y;
-    r.w[2] = v.z;
-    r.w[3] = v.w;
+    RawU8 r;
+    r.v = active ? __ldg(reinterpret_cast<const uint4*>(p + x0)) : make_uint4(0, 0, 0, 0);
+    r.lw = lane == 0 ? (uint32_t)__ldg(p + (x0 == 0 ? nx - 1 : x0 - 1)) << 24 : 0u;
+    r.rw = (active && (lane == 31 || x0 + 16 >= nx)) ? (uint32_t)__ldg(p + (x0 + 16 >= nx ? 0 : x0 + 16)) : 0u;
+    return r;
+}
+
+__device__ __forceinline__ RowU8 finish_row_u8(const RawU8& raw, int x0, int nx, int lane)
+{
+    uint32_t lw = __shfl_up_sync(FULL, raw.v.w, 1);
+    uint32_t rw = __shfl_down_sync(FULL, raw.v.x, 1);
+    if (lane == 0) lw = raw.lw;
+    if (lane == 31 || x0 + 16 >= nx) rw = raw.rw;
+    RowU8 r;
+    r.w[0] = raw.v.x;
+    r.w[1] = raw.v.y;
+    r.w[2] = raw.v.z;
+    r.w[3] = raw.v.w;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         uint32_t prev = k == 0 ? lw : r.w[k - 1];
         uint32_t next = k == 3 ? rw : r.w[k + 1];
-        uint32_t L = (r.w[k] << 8) | (prev >> 24);
-        uint32_t R = (r.w[k] >> 8) | (next << 24);
+        uint32_t L = __funnelshift_l(prev, r.w[k], 8);  // (w << 8) | (prev >> 24)
+        uint32_t R = __funnelshift_r(r.w[k], next, 8);  // (w >> 8) | (next << 24)
         r.s3[k] = L + r.w[k] + R;
     }
+    return r;
 }
 
-// Each warp task: a 512-byte strip (32 lanes x 16 cells) over LIFE_ROWS rows.
+// Warp tasks: a 512-byte strip (32 lanes x 16 cells) over LIFE_ROWS rows, visited grid-stride by
+// a grid sized to the resident capacity.  The loads of row j+2 (cur) and j+1 (old) are issued
+// before row j is computed, so two rows of loads are in flight per lane.
 template <int RULE>
 __global__ void __launch_bounds__(256) life_u8_swar(const uint8_t* __restrict__ cur, uint8_t* __restrict__ out,
                                                      int nx, int ny, int strips, int tasks)
 {
     const int lane = threadIdx.x & 31;
-    const int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (task >= tasks) return;  // warp-uniform
-    const int strip = task % strips, seg = task / strips;
-    const int x0 = strip * 512 + lane * 16;
-    const bool active = x0 < nx;
-    const int j0 = seg * LIFE_ROWS, j1 = min(j0 + LIFE_ROWS, ny);
-
-    RowU8 up, mid, dn;
-    load_row_u8(cur, nx, j0 == 0 ? ny - 1 : j0 - 1, x0, active, lane, up);
-    load_row_u8(cur, nx, j0, x0, active, lane, mid);
-    for (int j = j0; j < j1; j++) {
-        load_row_u8(cur, nx, j == ny - 1 ? 0 : j + 1, x0, active, lane, dn);
-        uint8_t* po = out + (size_t)j * nx + x0;
-        if (active) {
-            uint4 o = make_uint4(0, 0, 0, 0);
-            if (RULE == APPFIS_GB_LIFE_REFERENCE) o = *reinterpret_cast<const uint4*>(po);
-            uint32_t ow[4] = {o.x, o.y, o.z, o.w}, nw[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                uint32_t cnt = up.s3[k] + (mid.s3[k] - mid.w[k]) + dn.s3[k];
-                nw[k] = rule_bytes<RULE>(cnt, mid.w[k], ow[k]);
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < tasks; task += nwarps) {
+        const int strip = task % strips, seg = task / strips;
+        const int x0 = strip * 512 + lane * 16;
+        const bool active = x0 < nx;
+        const int j0 = seg * LIFE_ROWS, j1 = min(j0 + LIFE_ROWS, ny);
+        RowU8 up = finish_row_u8(load_raw_u8(cur, nx, j0 == 0 ? ny - 1 : j0 - 1, x0, active, lane), x0, nx, lane);
+        RowU8 mid = finish_row_u8(load_raw_u8(cur, nx, j0, x0, active, lane), x0, nx, lane);
+        RawU8 rdn = load_raw_u8(cur, nx, j0 == ny - 1 ? 0 : j0 + 1, x0, active, lane);
+        uint4 o = (RULE == APPFIS_GB_LIFE_REFERENCE && active) ? *reinterpret_cast<const uint4*>(out + (size_t)j0 * nx + x0)
+                                                                : make_uint4(0, 0, 0, 0);
+        for (int j = j0; j < j1; j++) {
+            RawU8 rnext = {make_uint4(0, 0, 0, 0), 0u, 0u};
+            uint4 onext = make_uint4(0, 0, 0, 0);
+            if (j + 1 < j1) {  // prefetch (warp-uniform)
+                const int r2 = j + 2 >= ny ? j + 2 - ny : j + 2;
+                rnext = load_raw_u8(cur, nx, r2, x0, active, lane);
+                if (RULE == APPFIS_GB_LIFE_REFERENCE && active)
+                    onext = *reinterpret_cast<const uint4*>(out + (size_t)(j + 1) * nx + x0);
             }
-            *reinterpret_cast<uint4*>(po) = make_uint4(nw[0], nw[1], nw[2], nw[3]);
+            const RowU8 dn = finish_row_u8(rdn, x0, nx, lane);
+            if (active) {
+                const uint32_t ow[4] = {o.x, o.y, o.z, o.w};
+                uint32_t nw[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const uint32_t cnt = up.s3[k] + (mid.s3[k] - mid.w[k]) + dn.s3[k];
+                    nw[k] = rule_bytes<RULE>(cnt, mid.w[k], ow[k]);
+                }
+                *reinterpret_cast<uint4*>(out + (size_t)j * nx + x0) = make_uint4(nw[0], nw[1], nw[2], nw[3]);
+            }
+            up = mid;
+            mid = dn;
+            rdn = rnext;
+            o = onext;
         }
-        up = mid;
-        mid = dn;
     }
 }
 
@@ -136,56 +162,78 @@ struct RowBits {
     uint32_t a0, a1;  // left + self + right as 2-bit slices
     uint32_t h0, h1;  // left + right as 2-bit slices
 };
+struct RawBits {
+    uint32_t w, lw, rw;
+};
 
-__device__ __forceinline__ void load_row_bits(const uint32_t* __restrict__ bits, int nw, int row, int xw, bool active,
-                                              int lane, RowBits& r)
+__device__ __forceinline__ RawBits load_raw_bits(const uint32_t* __restrict__ bits, int nw, int row, int xw, bool active,
+                                                 int lane)
 {
     const uint32_t* p = bits + (size_t)row * nw;
-    uint32_t w = active ? __ldg(p + xw) : 0u;
-    uint32_t lw = __shfl_up_sync(FULL, w, 1);
-    uint32_t rw = __shfl_down_sync(FULL, w, 1);
-    if (lane == 0) lw = __ldg(p + (xw == 0 ? nw - 1 : xw - 1));
-    if (active && (lane == 31 || xw + 1 >= nw)) rw = __ldg(p + (xw + 1 >= nw ? 0 : xw + 1));
-    uint32_t L = (w << 1) | (lw >> 31);  // bit b = cell x-1
-    uint32_t R = (w >> 1) | (rw << 31);  // bit b = cell x+1
+    RawBits r;
+    r.w = active ? __ldg(p + xw) : 0u;
+    r.lw = lane == 0 ? __ldg(p + (xw == 0 ? nw - 1 : xw - 1)) : 0u;
+    r.rw = (active && (lane == 31 || xw + 1 >= nw)) ? __ldg(p + (xw + 1 >= nw ? 0 : xw + 1)) : 0u;
+    return r;
+}
+
+__device__ __forceinline__ RowBits finish_row_bits(const RawBits& raw, int xw, int nw, int lane)
+{
+    uint32_t lw = __shfl_up_sync(FULL, raw.w, 1);
+    uint32_t rw = __shfl_down_sync(FULL, raw.w, 1);
+    if (lane == 0) lw = raw.lw;
+    if (lane == 31 || xw + 1 >= nw) rw = raw.rw;
+    const uint32_t w = raw.w;
+    const uint32_t L = __funnelshift_l(lw, w, 1);  // bit b = cell x-1
+    const uint32_t R = __funnelshift_r(w, rw, 1);  // bit b = cell x+1
+    RowBits r;
     r.w = w;
     r.a0 = L ^ w ^ R;
     r.a1 = (L & w) | (R & (L ^ w));
     r.h0 = L ^ R;
     r.h1 = L & R;
+    return r;
 }
 
-// Each warp task: 32 words (1024 cells) per row over LIFE_ROWS rows.
+// Warp tasks: 32 words (1024 cells) per row over LIFE_ROWS rows, grid-stride, one row prefetched.
 template <int RULE>
 __global__ void __launch_bounds__(256) life_bits_sweep(const uint32_t* __restrict__ cur, uint32_t* __restrict__ out,
                                                         int nw, int ny, int strips, int tasks)
 {
     const int lane = threadIdx.x & 31;
-    const int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (task >= tasks) return;
-    const int strip = task % strips, seg = task / strips;
-    const int xw = strip * 32 + lane;
-    const bool active = xw < nw;
-    const int j0 = seg * LIFE_ROWS, j1 = min(j0 + LIFE_ROWS, ny);
-
-    RowBits up, mid, dn;
-    load_row_bits(cur, nw, j0 == 0 ? ny - 1 : j0 - 1, xw, active, lane, up);
-    load_row_bits(cur, nw, j0, xw, active, lane, mid);
-    for (int j = j0; j < j1; j++) {
-        load_row_bits(cur, nw, j == ny - 1 ? 0 : j + 1, xw, active, lane, dn);
-        if (active) {
-            uint32_t* po = out + (size_t)j * nw + xw;
-            uint32_t o = RULE == APPFIS_GB_LIFE_REFERENCE ? *po : 0u;
-            // count = up(3-input) + mid(2-input) + dn(3-input), bit-sliced
-            uint32_t t0 = up.a0 ^ mid.h0, c0 = up.a0 & mid.h0;
-            uint32_t t1 = up.a1 ^ mid.h1 ^ c0, t2 = (up.a1 & mid.h1) | (c0 & (up.a1 ^ mid.h1));
-            uint32_t r0 = t0 ^ dn.a0, k0 = t0 & dn.a0;
-            uint32_t r1 = t1 ^ dn.a1 ^ k0, k1 = (t1 & dn.a1) | (k0 & (t1 ^ dn.a1));
-            uint32_t r2 = t2 ^ k1, r3 = t2 & k1;
-            *po = rule_bits<RULE>(r0, r1, r2, r3, mid.w, o);
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < tasks; task += nwarps) {
+        const int strip = task % strips, seg = task / strips;
+        const int xw = strip * 32 + lane;
+        const bool active = xw < nw;
+        const int j0 = seg * LIFE_ROWS, j1 = min(j0 + LIFE_ROWS, ny);
+        RowBits up = finish_row_bits(load_raw_bits(cur, nw, j0 == 0 ? ny - 1 : j0 - 1, xw, active, lane), xw, nw, lane);
+        RowBits mid = finish_row_bits(load_raw_bits(cur, nw, j0, xw, active, lane), xw, nw, lane);
+        RawBits rdn = load_raw_bits(cur, nw, j0 == ny - 1 ? 0 : j0 + 1, xw, active, lane);
+        uint32_t o = (RULE == APPFIS_GB_LIFE_REFERENCE && active) ? out[(size_t)j0 * nw + xw] : 0u;
+        for (int j = j0; j < j1; j++) {
+            RawBits rnext = {0u, 0u, 0u};
+            uint32_t onext = 0u;
+            if (j + 1 < j1) {
+                const int r2 = j + 2 >= ny ? j + 2 - ny : j + 2;
+                rnext = load_raw_bits(cur, nw, r2, xw, active, lane);
+                if (RULE == APPFIS_GB_LIFE_REFERENCE && active) onext = out[(size_t)(j + 1) * nw + xw];
+            }
+            const RowBits dn = finish_row_bits(rdn, xw, nw, lane);
+            if (active) {
+                // count = up(3-input) + mid(2-input) + dn(3-input), bit-sliced
+                const uint32_t t0 = up.a0 ^ mid.h0, c0 = up.a0 & mid.h0;
+                const uint32_t t1 = up.a1 ^ mid.h1 ^ c0, t2 = (up.a1 & mid.h1) | (c0 & (up.a1 ^ mid.h1));
+                const uint32_t r0 = t0 ^ dn.a0, k0 = t0 & dn.a0;
+                const uint32_t r1 = t1 ^ dn.a1 ^ k0, k1 = (t1 & dn.a1) | (k0 & (t1 ^ dn.a1));
+                const uint32_t r2 = t2 ^ k1, r3 = t2 & k1;
+                out[(size_t)j * nw + xw] = rule_bits<RULE>(r0, r1, r2, r3, mid.w, o);
+            }
+            up = mid;
+            mid = dn;
+            rdn = rnext;
+            o = onext;
         }
-        up = mid;
-        mid = dn;
     }
 }
 
@@ -250,6 +298,16 @@ __global__ void popcount_tail(const uint8_t* __restrict__ p, int n, unsigned lon
     if (s) atomicAdd(out, s);
 }
 
+// Blocks of 256 threads: as many as are resident at once, but no more than the warp tasks need.
+template <class K>
+unsigned resident_grid(K kernel, int tasks)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess || per_sm < 1) per_sm = 4;
+    const size_t need = gb::ceil_div((size_t)tasks * 32, 256);
+    return (unsigned)std::max<size_t>(1, std::min<size_t>(need, (size_t)per_sm * gb::sm_count()));
+}
+
 template <int RULE>
 int run_u8(uint8_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStream_t st)
 {
@@ -257,7 +315,7 @@ int run_u8(uint8_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStream
     if (nx % 16 == 0) {
         const int strips = (nx + 511) / 512;
         const int tasks = strips * ((ny + LIFE_ROWS - 1) / LIFE_ROWS);
-        const unsigned grid = gb::ceil_div((size_t)tasks * 32, 256);
+        const unsigned grid = resident_grid(life_u8_swar<RULE>, tasks);
         for (int g = 0; g < gens; g++) {
             life_u8_swar<RULE><<<grid, 256, 0, st>>>(buf[ci], buf[1 - ci], nx, ny, strips, tasks);
             ci = 1 - ci;
@@ -280,7 +338,7 @@ int run_bits(uint32_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStr
     const int nw = nx / 32;
     const int strips = (nw + 31) / 32;
     const int tasks = strips * ((ny + LIFE_ROWS - 1) / LIFE_ROWS);
-    const unsigned grid = gb::ceil_div((size_t)tasks * 32, 256);
+    const unsigned grid = resident_grid(life_bits_sweep<RULE>, tasks);
     int ci = 0;
     for (int g = 0; g < gens; g++) {
         life_bits_sweep<RULE><<<grid, 256, 0, st>>>(buf[ci], buf[1 - ci], nw, ny, strips, tasks);

@@ -110,7 +110,8 @@ def himeno_p(nx, ny, nz, dtype=np.float32):
     """padded p: (k/(kmax-1))^2 along z over the interior, zero ghost ring."""
     p = np.zeros((nz + 2, ny + 2, nx + 2), dtype=dtype)
     k = np.arange(nz, dtype=np.float64)
-    prof = (k / (nz - 1)) ** 2 if dtype == np.float64 else (k.astype(np.float32) / np.float32(nz - 1)) ** 2
+    den = max(nz - 1, 1)
+    prof = (k / den) ** 2 if dtype == np.float64 else (k.astype(np.float32) / np.float32(den)) ** 2
     p[1:-1, 1:-1, 1:-1] = prof.astype(dtype)[:, None, None]
     return p
 

@@ -79,6 +79,14 @@ APPFIS_GB_API int appfis_gb_reduce(const void* field, int dtype, int px, int py,
 APPFIS_GB_API int appfis_gb_reduce_host(const void* field, int dtype, int px, int py, const int* box, int op, double* result,
                           void* stream);
 
+/* ----------------------------------------------------------------------------- halo */
+/* Periodic ghost refresh of a dense padded field (row pitch = padded_dims[0]) in place: the
+ * single-rank form of Exchange for periodic grids (Appfis/Communication.hpp:612-678 with the
+ * pack/unpack of Appfis/Runtime.hpp:916-1173), axis by axis over full faces so corners match.
+ * elem_size 1, 2, 4 or 8 bytes; each padded axis must be >= 3*ghost. */
+APPFIS_GB_API int appfis_gb_ghost_periodic(void* field, int elem_size, int ndim, const int* padded_dims, int ghost,
+                                           void* stream);
+
 /* ----------------------------------------------------------------------------- GameOfLife */
 /* Replaces Execute2D(config, cur, next) with the GameOfLife functor + the periodic halo
  * exchange per generation (GameOfLife/src/game_appfis.hpp:79-82,121-135;
@@ -137,13 +145,13 @@ APPFIS_GB_API int appfis_gb_heat2d_job(float* field, int nx, int ny, int iters, 
  * double inside the sweep (deterministic order); the reference computes no gosa. */
 APPFIS_GB_API int appfis_gb_himeno(const float* const* coef, float* p, float* wrk2, int nx, int ny, int nz, int pitch,
                                    int iters, float omega, double* dev_gosa, int* cur_index, void* stream);
-/* Mixed-precision defect correction: FP16 storage of the correction e, the defect D and ten
- * folded weights (26 B per point per sweep instead of 56), FP32 arithmetic, FP32 master p
- * refreshed every `period` sweeps (the defect D = omega*ss(p) is then recomputed from the FP32
- * coefficients).  Same iteration as appfis_gb_himeno in exact arithmetic; the difference is
- * the FP16 rounding of the last period's correction.  p_work: a second FP32 field;
- * half_work: 13 FP16 fields (13 * pitch*(ny+2)*(nz+2) halves).  gosa as above (from the FP16
- * iterate, FP32 ss, double sum). */
+/* Mixed-precision defect correction: FP16 storage of the correction e, the defect D and the ten
+ * neighbour/boundary coefficient fields, a3 read in FP32 (30 B per point per sweep instead of 56),
+ * FP32 arithmetic, FP32 master p refreshed every `period` sweeps (the defect D = omega*ss(p) is
+ * then recomputed from the FP32 coefficients).  Same iteration as appfis_gb_himeno in exact
+ * arithmetic; the difference is the FP16 rounding inside one period.  p_work: a second FP32
+ * field; half_work: 13 FP16 fields (13 * pitch*(ny+2)*(nz+2) halves).  gosa as above (from the
+ * FP16 iterate, FP32 ss, double sum). */
 APPFIS_GB_API int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, void* half_work, int nx, int ny,
                                          int nz, int pitch, int iters, int period, float omega, double* dev_gosa,
                                          int* cur_index, void* stream);

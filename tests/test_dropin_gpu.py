@@ -1,0 +1,101 @@
+"""The drop-in C++ API (appfis_gb300/Appfis: Grid / Config / Execute*D / Execute*DReduce /
+HaloExchange / Scatter / Gather) on the GPU: application-style functors driven through it give
+the reference's results (golden fixtures from the reference's own CPU path, and the oracle)."""
+import glob
+import json
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from appfis_gb300 import workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module")
+def runner(gb):
+    from tests.dropin import build_runner
+    return build_runner.build()
+
+
+def run(exe, args, inputs, outputs):
+    with tempfile.TemporaryDirectory() as td:
+        subs = {}
+        for k, a in enumerate(inputs):
+            p = os.path.join(td, "in%d" % k)
+            np.ascontiguousarray(a).tofile(p)
+            subs["in%d" % k] = p
+        for k in range(len(outputs)):
+            subs["out%d" % k] = os.path.join(td, "out%d" % k)
+        r = subprocess.run([exe] + [str(a).format(**subs) for a in args], capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+        res = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+        return res, [np.fromfile(subs["out%d" % k], dtype=dt) for k, dt in enumerate(outputs)]
+
+
+@pytest.mark.parametrize("f", sorted(glob.glob(os.path.join(GOLD, "gol_*.npz"))), ids=os.path.basename)
+def test_gol_golden(runner, f):
+    g = np.load(f)
+    ny, nx = g["cells"].shape
+    res, (out,) = run(runner, ["gol", nx, ny, int(g["gens"]), "{in0}", "{out0}"], [g["cells"]], [np.uint8])
+    assert np.array_equal(out.reshape(ny, nx), g["out"])
+    assert res["live"] == int(g["live"])
+
+
+def test_gol_larger_vs_oracle(runner):
+    c = W.gol_cells(300, 170, 0.3, 12)
+    res, (out,) = run(runner, ["gol", 300, 170, 40, "{in0}", "{out0}"], [c], [np.uint8])
+    ref, _ = O.gol(c, 40)
+    assert np.array_equal(out.reshape(170, 300), ref) and res["live"] == int(ref.sum())
+
+
+@pytest.mark.parametrize("f", sorted(glob.glob(os.path.join(GOLD, "heat2d_*.npz"))), ids=os.path.basename)
+def test_heat2d_golden(runner, f):
+    g = np.load(f)
+    ny, nx = g["padded"].shape[0] - 2, g["padded"].shape[1] - 2
+    res, (out,) = run(runner, ["heat2d", nx, ny, int(g["iters"]), 0.2, 1.0, "{in0}", "{out0}"],
+                      [np.ascontiguousarray(g["padded"][1:-1, 1:-1])], [np.float32])
+    assert np.array_equal(out.reshape(ny + 2, nx + 2), g["out"])
+    assert np.float32(res["max"]) == np.float32(g["stats"][0])
+    assert np.float32(res["min"]) == np.float32(g["stats"][1])
+    assert abs(res["sum"] - g["stats"][2]) <= 1e-5 * abs(g["stats"][2])
+
+
+@pytest.mark.parametrize("f", sorted(glob.glob(os.path.join(GOLD, "himeno_*.npz"))), ids=os.path.basename)
+def test_himeno_golden(runner, f):
+    g = np.load(f)
+    p = g["p"]
+    nz, ny, nx = p.shape[0] - 2, p.shape[1] - 2, p.shape[2] - 2
+    res, (out,) = run(runner, ["himeno", nx, ny, nz, int(g["iters"]), 0.8, "{in0}", "{in1}", "{out0}"],
+                      [g["coef"], np.ascontiguousarray(p[1:-1, 1:-1, 1:-1])], [np.float32])
+    assert np.array_equal(out.reshape(p.shape), g["out"])
+
+
+@pytest.mark.parametrize("f", sorted(glob.glob(os.path.join(GOLD, "fdtd_*.npz"))), ids=os.path.basename)
+def test_fdtd_golden(runner, f):
+    g = np.load(f)
+    pd = g["padded"]
+    nz, ny, nx = pd.shape[0] - 8, pd.shape[1] - 8, pd.shape[2] - 8
+    res, (out,) = run(runner, ["fdtd", nx, ny, nz, int(g["iters"]), float(g["coeff"]), "{in0}", "{out0}"],
+                      [np.ascontiguousarray(pd[4:-4, 4:-4, 4:-4])], [np.float32])
+    assert np.array_equal(out.reshape(pd.shape), g["out"])
+
+
+@pytest.mark.parametrize("f", sorted(glob.glob(os.path.join(GOLD, "triton_*.npz"))), ids=os.path.basename)
+def test_triton_golden(runner, f):
+    g = np.load(f)
+    ny, nx = g["dem"].shape
+    dx, cn, hextra, mann, t_end, pint, ts = [float(v) for v in g["params"]]
+    res, (out, dts) = run(runner, ["triton", nx, ny, dx, cn, hextra, mann, t_end, pint, ts, int(g["steps"]), "{in0}", "{in1}",
+                                   "{out0}", "{out1}"], [g["dem"], g["h0"]], [np.float64, np.float64])
+    n = nx * ny
+    assert res["steps"] == int(g["steps"])
+    np.testing.assert_allclose(dts, g["dts"], rtol=1e-9)
+    np.testing.assert_allclose(out[:n].reshape(ny, nx), g["h"], atol=1e-9)
+    np.testing.assert_allclose(out[n:2 * n].reshape(ny, nx), g["qx"], atol=1e-9)
+    np.testing.assert_allclose(out[2 * n:].reshape(ny, nx), g["qy"], atol=1e-9)
