@@ -12,6 +12,12 @@ int run_f64(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_
     return run<double>(doms, ndom, prm, dtlog, steps, simtime, status, st);
 }
 
+int setup_f64(const appfis_gb_flood_domain* dom, const double* dem, const double* h, const double* qx, const double* qy,
+              double manning, cudaStream_t st)
+{
+    return setup<double>(dom, dem, h, qx, qy, manning, st);
+}
+
 int job_f64(int ndom, const int* nx, const int* ny, const double* const* dem, double* const* h, double* const* qx,
             double* const* qy, double manning, const appfis_gb_flood_params* prm, int* steps_out, double* mass_out,
             double* dtlog_host)

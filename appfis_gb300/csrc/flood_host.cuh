@@ -89,6 +89,19 @@ int make_table(const appfis_gb_flood_domain* doms, int ndom, std::vector<Dom<T>>
     return APPFIS_GB_OK;
 }
 
+// Initialises one domain's device buffers from FP64 device interiors (nx*ny each).
+template <class T>
+int setup(const appfis_gb_flood_domain* dom, const double* dem, const double* h, const double* qx, const double* qy,
+          double manning, cudaStream_t st)
+{
+    if (!dom || !dem || !h) return gb::fail(APPFIS_GB_EINVAL, "flood_setup: null argument");
+    std::vector<Dom<T>> one;
+    long long tot;
+    GB_TRY(make_table<T>(dom, 1, one, tot));
+    flood_setup<T><<<dim3(gb::ceil_div(dom->nx + 2, 128), dom->ny + 2), 128, 0, st>>>(one[0], dem, h, qx, qy, manning);
+    return gb::launched("flood_setup");
+}
+
 // Uploads the table, initialises the control block and launches the persistent kernel.
 template <class T>
 int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_params* prm, double* dev_dtlog, int* dev_steps,

@@ -216,6 +216,11 @@ typedef struct {
 APPFIS_GB_API int appfis_gb_flood_run(const appfis_gb_flood_domain* doms, int ndom, int dtype,
                                       const appfis_gb_flood_params* prm, double* dev_dtlog, int* dev_steps,
                                       double* dev_simtime, int* dev_status, void* stream);
+/* Initialises one domain's buffers (both state buffers, dem with a 1e6 ghost ring as the reference's
+ * dem.SetBoundary(1e6), n2 = manning^2 everywhere) from FP64 DEVICE interiors dem, h, qx, qy
+ * (nx*ny each; qx/qy may be NULL = 0). */
+APPFIS_GB_API int appfis_gb_flood_setup(const appfis_gb_flood_domain* dom, int dtype, const double* dem, const double* h,
+                                        const double* qx, const double* qy, double manning, void* stream);
 /* Host-buffer job: per domain nx*ny FP64 interiors dem[d], h[d] (in/out), qx[d]/qy[d] (in/out,
  * may be NULL = zero initial momentum, not returned); computed in `dtype`.  steps_out (ndom),
  * mass_out (2*ndom: sum of h over the interior before and after, FP64), dtlog_host (ndom*max_steps)
