@@ -30,6 +30,7 @@ SIGNATURES = {
     "appfis_gb_stream_sync": [_P],
     "appfis_gb_reduce": [_P, _i, _i, _i, _P, _i, _P, _P],
     "appfis_gb_reduce_host": [_P, _i, _i, _i, _P, _i, _P, _P],
+    "appfis_gb_reduce_noalloc": [_P, _i, _i, _i, _P, _i, _P, _P],
     "appfis_gb_ghost_periodic": [_P, _i, _i, _P, _i, _P],
     "appfis_gb_life_u8": [_P, _P, _i, _i, _i, _i, _P, _P],
     "appfis_gb_life_pack": [_P, _P, _i, _i, _P],

@@ -13,6 +13,7 @@
 // make the result deterministic; floating sums accumulate in double.  The input is never written.
 #include <cfloat>
 #include <climits>
+#include <mutex>
 #include <type_traits>
 
 #include "gb_common.cuh"
@@ -122,9 +123,92 @@ int launch_reduce(const void* field, int px, int py, const int* b, int op, void*
     return gb::launched("reduce_box");
 }
 
+// ---------------------------------------------------------------- allocation-free variant
+// Some callers cannot allocate device memory at the moment they need a reduction: code that
+// runs while a stream is being captured into a CUDA graph (an allocation there fails or breaks
+// the capture), code inside a host framework whose allocator has reserved all device memory,
+// or a latency-critical loop where the synchronising cudaMalloc/cudaFree of a first call is not
+// acceptable.  For them the same reduction kernel can take its scratch (one ticket counter and
+// one partial per block) from a fixed array that is part of the library image instead of the
+// grow-only workspace.  64 KiB holds the ticket and 8160 partials; the kernel uses at most
+// 4 blocks per SM (608 on a GB300), so every box fits on current GPUs.  Every device that loads
+// the library keeps this array until the process exits.
+constexpr size_t NOALLOC_SCRATCH_BYTES = 64 * 1024;
+constexpr size_t NOALLOC_MAX_PARTIALS = (NOALLOC_SCRATCH_BYTES - 256) / sizeof(double);
+static __device__ __align__(256) unsigned char g_reduce_scratch[NOALLOC_SCRATCH_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of the scratch array on the current device.  On the host the array's name
+// only stands for the symbol, so its address is looked up once per device (first call on that
+// device, with it current) and cached.
+int noalloc_scratch(void** out)
+{
+    int dev = 0;
+    GB_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return gb::fail(APPFIS_GB_EINVAL, "reduce_noalloc: device %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_reduce_scratch);
+        if (e != cudaSuccess || !p) return gb::cuda_status(e != cudaSuccess ? e : cudaErrorInvalidSymbol, "cudaGetSymbolAddress(reduce scratch)");
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return APPFIS_GB_OK;
+}
+
+template <class T>
+int launch_reduce_noalloc(const void* field, int px, int py, const int* b, int op, void* res, cudaStream_t st)
+{
+    typedef typename Acc<T>::type A;
+    const long long rows = (long long)(b[3] - b[2]) * (b[5] - b[4]);
+    const int grid = (int)std::max<long long>(1, std::min<long long>(rows, (long long)gb::sm_count() * 4));
+    if ((size_t)grid > NOALLOC_MAX_PARTIALS)
+        return gb::fail(APPFIS_GB_EINVAL, "reduce_noalloc: %d partial sums needed, the fixed scratch holds %zu", grid,
+                        NOALLOC_MAX_PARTIALS);
+    void* ws = nullptr;
+    GB_TRY(noalloc_scratch(&ws));
+    unsigned* ticket = reinterpret_cast<unsigned*>(ws);
+    A* partials = reinterpret_cast<A*>(reinterpret_cast<char*>(ws) + 256);
+    GB_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned), st));  // the array keeps the last call's contents
+    const T* f = reinterpret_cast<const T*>(field);
+    switch (op) {
+    case APPFIS_GB_MAX:
+        reduce_box<T, APPFIS_GB_MAX><<<grid, RED_THREADS, 0, st>>>(f, px, py, b[0], b[1], b[2], b[3], b[4], b[5], partials, ticket, res);
+        break;
+    case APPFIS_GB_MIN:
+        reduce_box<T, APPFIS_GB_MIN><<<grid, RED_THREADS, 0, st>>>(f, px, py, b[0], b[1], b[2], b[3], b[4], b[5], partials, ticket, res);
+        break;
+    default:
+        reduce_box<T, APPFIS_GB_SUM><<<grid, RED_THREADS, 0, st>>>(f, px, py, b[0], b[1], b[2], b[3], b[4], b[5], partials, ticket, res);
+    }
+    return gb::launched("reduce_box (fixed scratch)");
+}
+
 }  // namespace
 
 extern "C" {
+
+int appfis_gb_reduce_noalloc(const void* field, int dtype, int px, int py, const int* box, int op, void* dev_result,
+                             void* stream)
+{
+    if (!field || !box || !dev_result) return gb::fail(APPFIS_GB_EINVAL, "reduce_noalloc: null argument");
+    if (op < APPFIS_GB_MAX || op > APPFIS_GB_SUM) return gb::fail(APPFIS_GB_EINVAL, "reduce_noalloc: unknown op %d", op);
+    for (int a = 0; a < 3; a++)
+        if (box[2 * a] < 0 || box[2 * a + 1] < box[2 * a]) return gb::fail(APPFIS_GB_EINVAL, "reduce_noalloc: bad box axis %d", a);
+    if (box[1] > px || box[3] > py || px < 1 || py < 1) return gb::fail(APPFIS_GB_EINVAL, "reduce_noalloc: box outside the field");
+    if (box[0] == box[1] || box[2] == box[3] || box[4] == box[5]) return gb::fail(APPFIS_GB_EINVAL, "reduce_noalloc: empty box");
+    cudaStream_t st = gb::as_stream(stream);
+    switch (dtype) {
+    case APPFIS_GB_F32: return launch_reduce_noalloc<float>(field, px, py, box, op, dev_result, st);
+    case APPFIS_GB_F64: return launch_reduce_noalloc<double>(field, px, py, box, op, dev_result, st);
+    case APPFIS_GB_I32: return launch_reduce_noalloc<int32_t>(field, px, py, box, op, dev_result, st);
+    default: return gb::fail(APPFIS_GB_EINVAL, "reduce_noalloc: unknown dtype %d", dtype);
+    }
+}
 
 int appfis_gb_reduce(const void* field, int dtype, int px, int py, const int* box, int op, void* dev_result, void* stream)
 {

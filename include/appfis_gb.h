@@ -75,6 +75,19 @@ APPFIS_GB_API int appfis_gb_stream_sync(void* stream);
  * (fixed-order tree: per-block partials, then the last block folds them in block order). */
 APPFIS_GB_API int appfis_gb_reduce(const void* field, int dtype, int px, int py, const int* box, int op, void* dev_result,
                      void* stream);
+/* Same reduction, same result, for callers that must not allocate device memory — e.g. code
+ * running while a stream is captured into a CUDA graph, inside a framework whose allocator has
+ * reserved the device memory, or in a loop that cannot afford a synchronising cudaMalloc.  No
+ * counterpart in the reference (its reductions allocate nothing beyond the grid's own buffers).
+ * The scratch (a ticket and one partial sum per block) lives in a fixed 64 KiB device array
+ * inside the library, held by every device that loads it until the process exits; a box whose
+ * reduction needs more than 8160 partial sums is rejected with APPFIS_GB_EINVAL (this kernel
+ * uses at most 4 per SM).  Nothing is allocated: the first call on a device looks up the array's
+ * device address with that device current (make that first call before any stream capture);
+ * every call clears the ticket with an asynchronous memset on `stream`.  All calls share the
+ * array, so calls that overlap on the GPU (other streams, other host threads) race: order them. */
+APPFIS_GB_API int appfis_gb_reduce_noalloc(const void* field, int dtype, int px, int py, const int* box, int op,
+                                           void* dev_result, void* stream);
 /* Same, returning the value on the host (synchronises `stream`). */
 APPFIS_GB_API int appfis_gb_reduce_host(const void* field, int dtype, int px, int py, const int* box, int op, double* result,
                           void* stream);
