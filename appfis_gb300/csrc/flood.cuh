@@ -265,14 +265,15 @@ __global__ void __launch_bounds__(256) flood_persistent(const Dom<T>* __restrict
         // phase B
         for (long long s = warp; s < p.total_strips; s += nwarps) {
             const int d = find_domain(doms, p.ndom, s);
-            if (is_active(ctl, cur, d, p) && step_dt(ctl, cur, d, p, big) > 0.0)
+            if (is_active(ctl, cur, d, p) && step_dt(ctl, cur, d, p, big) > 1e-9 * p.time_step)
                 phase_b<T>(doms[d], ctl, cur, d, s - doms[d].strip0, p);
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) {  // commit the per-domain scalars of step n
             for (int d = 0; d < p.ndom; d++) {
                 if (is_active(ctl, cur, d, p)) {
                     const double dt = step_dt(ctl, cur, d, p, big);
-                    if (!(dt > 0.0)) atomicExch(&ctl->error, 2);  // collapsed or NaN time step: stop the run
+                    // a collapsed (below 1e-9 of the step scale) or NaN time step stops the run
+                    if (!(dt > 1e-9 * p.time_step)) atomicExch(&ctl->error, 2);
                     const double st = ctl->simtime[cur][d] + dt;
                     int pid = ctl->pid[cur][d];
                     if (st >= p.print_interval * (pid + 1)) pid++;

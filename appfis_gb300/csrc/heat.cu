@@ -35,6 +35,7 @@ __global__ void __launch_bounds__(256) heat2d_sweep_k(const float* __restrict__ 
 }
 
 // Overlapped tiling: output tile TX x TY, halo S (runtime, <= SMAX), S sweeps per launch.
+// Threads form a 32 x 8 grid that strides over the shared region (no index division).
 template <int TX, int TY, int SMAX>
 __global__ void __launch_bounds__(256) heat2d_blocked(const float* __restrict__ cur, float* __restrict__ nxt, int nx,
                                                        int ny, int pitch, int S, float cx, float cy)
@@ -46,39 +47,55 @@ __global__ void __launch_bounds__(256) heat2d_blocked(const float* __restrict__ 
     const int rw = TX + 2 * S, rh = TY + 2 * S;  // region actually used
     const int ox = 1 + blockIdx.x * TX - S;      // padded coords of region (0,0)
     const int oy = 1 + blockIdx.y * TY - S;
-    const int tid = threadIdx.x;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
 
-    for (int e = tid; e < rw * rh; e += blockDim.x) {
-        const int ry = e / rw, rx = e - ry * rw;
-        const int gx = ox + rx, gy = oy + ry;
-        float v = 0.0f;
-        if (gx >= 0 && gx <= nx + 1 && gy >= 0 && gy <= ny + 1) v = __ldg(cur + (size_t)gy * pitch + gx);
-        A[ry * RW + rx] = v;
-        B[ry * RW + rx] = v;  // ghost / outside cells keep their value in both buffers
-    }
+    // load the region: all loads of a thread are issued before any is stored (one L2 round trip)
+    constexpr int LR = (RH + 7) / 8, LC = (RW + 31) / 32;
+    float v[LR][LC];
+#pragma unroll
+    for (int a = 0; a < LR; a++)
+#pragma unroll
+        for (int c = 0; c < LC; c++) {
+            const int ry = ty + 8 * a, rx = tx + 32 * c, gy = oy + ry, gx = ox + rx;
+            v[a][c] = (ry < rh && rx < rw && gx >= 0 && gx <= nx + 1 && gy >= 0 && gy <= ny + 1)
+                          ? __ldg(cur + (size_t)gy * pitch + gx) : 0.0f;
+        }
+#pragma unroll
+    for (int a = 0; a < LR; a++)
+#pragma unroll
+        for (int c = 0; c < LC; c++) {
+            const int ry = ty + 8 * a, rx = tx + 32 * c;
+            if (ry < rh && rx < rw) {
+                A[ry * RW + rx] = v[a][c];
+                B[ry * RW + rx] = v[a][c];  // ghost / outside cells keep their value in both buffers
+            }
+        }
     __syncthreads();
 
+    // interior cells of the region (those updated by the sweep), in region coordinates
+    const int ix0 = max(1 - ox, 0), ix1 = min(nx + 1 - ox, rw);  // gx in [1, nx]
+    const int iy0 = max(1 - oy, 0), iy1 = min(ny + 1 - oy, rh);
     for (int s = 1; s <= S; s++) {
         // valid after this sweep: region cells [s, rw-s) x [s, rh-s)
-        const int w = rw - 2 * s, h = rh - 2 * s;
-        for (int e = tid; e < w * h; e += blockDim.x) {
-            const int ry = s + e / w, rx = s + (e - (e / w) * w);
-            const int gx = ox + rx, gy = oy + ry;
-            if (gx >= 1 && gx <= nx && gy >= 1 && gy <= ny) {
+        const int x0 = max(s, ix0), x1 = min(rw - s, ix1), y0 = max(s, iy0), y1 = min(rh - s, iy1);
+        for (int ry = y0 + ty; ry < y1; ry += 8)
+            for (int rx = x0 + tx; rx < x1; rx += 32) {
                 const int q = ry * RW + rx;
                 B[q] = heat_point(A[q], A[q - 1], A[q + 1], A[q - RW], A[q + RW], cx, cy);
             }
-        }
         __syncthreads();
         float* t = A;
         A = B;
         B = t;
     }
 
-    for (int e = tid; e < TX * TY; e += blockDim.x) {
-        const int ty = e / TX, tx = e - ty * TX;
-        const int gx = 1 + blockIdx.x * TX + tx, gy = 1 + blockIdx.y * TY + ty;
-        if (gx <= nx && gy <= ny) nxt[(size_t)gy * pitch + gx] = A[(ty + S) * RW + (tx + S)];
+    for (int y = ty; y < TY; y += 8) {
+        const int gy = 1 + blockIdx.y * TY + y;
+        if (gy > ny) break;
+        for (int x = tx; x < TX; x += 32) {
+            const int gx = 1 + blockIdx.x * TX + x;
+            if (gx <= nx) nxt[(size_t)gy * pitch + gx] = A[(y + S) * RW + (x + S)];
+        }
     }
 }
 

@@ -5,10 +5,10 @@
 // on a DUAL p grid and 12 SINGLE coefficient grids (:74-86, :108-114).  The reference computes
 // no gosa; ss is exactly its :195 expression.
 //
-// Plain form: one launch per sweep.  A thread owns an (i, j) column and marches a chunk of z,
-// carrying p(k-1), p(k), p(k+1) in registers; the other 14 p neighbours come through L1.  The
-// 12 coefficient streams are read once.  The sum uses round-to-nearest intrinsics in the
-// reference's order (no FMA contraction), so p is bit-identical to the reference CPU path.
+// Plain form: one launch per sweep (himeno_ring<0>, below): 2.5-D z-march with the p planes in
+// a shared ring; the 12 coefficient streams are read once, one plane ahead.  The sum uses
+// round-to-nearest intrinsics in the reference's order (no FMA contraction), so p is
+// bit-identical to the reference CPU path.
 //
 // Defect-correction form (FP16 storage, FP32 arithmetic).  With p = P + e (P an FP32 master
 // frozen between corrections) the Jacobi update p' = p + w*bnd*(a3*(N p + wrk1) - p) becomes
@@ -21,6 +21,8 @@
 // which bounds the FP16 error to the last period's correction.  The sweep's own ss is
 // (e' - e)/w (FP32, before rounding e').
 #include <cuda_fp16.h>
+
+#include <type_traits>
 
 #include "gb_common.cuh"
 
@@ -91,40 +93,6 @@ __device__ __forceinline__ void gosa_reduce(double v, double* __restrict__ parti
                   fmul(C2, F(0, 0, -1))),                                                                                   \
          W1)
 
-template <int BX, int BY>
-__global__ void __launch_bounds__(BX* BY) himeno_sweep(Coef12 cf, const float* __restrict__ p, float* __restrict__ out,
-                                                        int nx, int ny, int nz, int px, int py, int kz, float omega,
-                                                        double* __restrict__ partials, unsigned* __restrict__ ticket,
-                                                        double* __restrict__ gosa)
-{
-    const int i = 1 + blockIdx.x * BX + threadIdx.x;
-    const int j = 1 + blockIdx.y * BY + threadIdx.y;
-    const int k0 = 1 + blockIdx.z * kz, k1 = min(k0 + kz, nz + 1);
-    const size_t plane = (size_t)px * py;
-    double g = 0.0;
-    if (i <= nx && j <= ny) {
-        size_t c = ((size_t)k0 * py + j) * px + i;
-        float pm = __ldg(p + c - plane), p0 = __ldg(p + c);
-        for (int k = k0; k < k1; k++) {
-            const float pp = __ldg(p + c + plane);
-#define PF(di, dj, dk)                                                                                             \
-    ((di) == 0 && (dj) == 0 ? ((dk) < 0 ? pm : ((dk) > 0 ? pp : p0))                                              \
-                            : __ldg(p + c + (ptrdiff_t)(di) + (ptrdiff_t)(dj) * px + (ptrdiff_t)(dk) * (ptrdiff_t)plane))
-            const float s0 = HIMENO_S0(PF, __ldg(cf.c[0] + c), __ldg(cf.c[1] + c), __ldg(cf.c[2] + c), __ldg(cf.c[4] + c),
-                                       __ldg(cf.c[5] + c), __ldg(cf.c[6] + c), __ldg(cf.c[7] + c), __ldg(cf.c[8] + c),
-                                       __ldg(cf.c[9] + c), __ldg(cf.c[11] + c));
-#undef PF
-            const float ss = fmul(fsub(fmul(s0, __ldg(cf.c[3] + c)), p0), __ldg(cf.c[10] + c));
-            out[c] = fadd(p0, fmul(omega, ss));
-            g += (double)ss * (double)ss;
-            pm = p0;
-            p0 = pp;
-            c += plane;
-        }
-    }
-    if (gosa) gosa_reduce(g, partials, ticket, gosa);
-}
-
 // ---------------------------------------------------------------- defect-correction form
 // FP16 copies of the ten neighbour / boundary coefficient fields (over the interior).
 __global__ void himeno_half_coef(Coef12 cf, __half* __restrict__ w, size_t field, int nx, int ny, int nz, int px, int py)
@@ -169,41 +137,152 @@ __global__ void __launch_bounds__(BX* BY) himeno_correct(Coef12 cf, const float*
     }
 }
 
-template <int BX, int BY>
-__global__ void __launch_bounds__(BX* BY) himeno_inner(H10 hf, const __half* __restrict__ e, const __half* __restrict__ D,
-                                                        __half* __restrict__ en, int nx, int ny, int nz, int px, int py,
-                                                        int kz, float omega, float inv_omega, double* __restrict__ partials,
-                                                        unsigned* __restrict__ ticket, double* __restrict__ gosa)
+// ---------------------------------------------------------------- 2.5-D forms with a shared plane ring
+// A CTA of RX x RY threads owns an (x, y) tile and marches a chunk of z.  p (or e) planes k-1,
+// k, k+1 live in a 4-slot shared ring with a one-cell x/y halo: plane k+2 is loaded into
+// registers one iteration ahead and written to its slot after the sweep of plane k, so one
+// barrier per plane suffices and every p value comes from memory once per CTA.  The point's
+// coefficients for plane k+1 are loaded while plane k is computed.  All neighbour reads are
+// shared-memory reads, so the only global traffic is the compulsory streams.
+constexpr int RX = 32, RY = 8;
+constexpr int RW = RX + 2, RH = RY + 2, RSLOT = RW * RH;
+constexpr int RHALO = RSLOT - RX * RY;  // 84 halo cells per plane
+
+// (row, col) in the slot of halo item h (0 <= h < RHALO): top row, bottom row, left col, right col
+__device__ __forceinline__ int halo_slot(int h)
 {
-    const int i = 1 + blockIdx.x * BX + threadIdx.x;
-    const int j = 1 + blockIdx.y * BY + threadIdx.y;
+    if (h < RW) return h;                                     // row 0
+    h -= RW;
+    if (h < RW) return (RH - 1) * RW + h;                     // row RH-1
+    h -= RW;
+    if (h < RY) return (h + 1) * RW;                          // col 0, rows 1..RY
+    h -= RY;
+    return (h + 1) * RW + RW - 1;                             // col RW-1
+}
+
+template <class L>
+__device__ __forceinline__ float ring_load(const L* f, size_t idx, bool ok);
+template <> __device__ __forceinline__ float ring_load<float>(const float* f, size_t idx, bool ok) { return ok ? __ldg(f + idx) : 0.0f; }
+template <> __device__ __forceinline__ float ring_load<__half>(const __half* f, size_t idx, bool ok)
+{
+    return ok ? __half2float(__ldg(f + idx)) : 0.0f;
+}
+
+// Loads plane k of field f for this thread: its centre value and (threads < RHALO) one halo value.
+template <class L>
+__device__ __forceinline__ void ring_fetch(const L* f, int k, int i, int j, int hi, int hj, int nx, int ny, int px,
+                                           size_t plane, int t, float& c, float& h)
+{
+    const size_t base = (size_t)k * plane;
+    c = ring_load<L>(f, base + (size_t)j * px + i, i <= nx + 1 && j <= ny + 1);
+    h = t < RHALO ? ring_load<L>(f, base + (size_t)hj * px + hi, hi <= nx + 1 && hj <= ny + 1) : 0.0f;
+}
+
+__device__ __forceinline__ void ring_store(float* slot, int t, int tx, int ty, int hs, float c, float h)
+{
+    slot[(ty + 1) * RW + tx + 1] = c;
+    if (t < RHALO) slot[hs] = h;
+}
+
+template <int MODE>  // 0: plain FP32 sweep of p; 1: FP16 correction sweep of e
+__global__ void __launch_bounds__(RX* RY) himeno_ring(Coef12 cf, H10 hf, const void* __restrict__ pin, void* __restrict__ pout,
+                                                       const __half* __restrict__ D, int nx, int ny, int nz, int px, int py,
+                                                       int kz, float omega, float inv_omega, double* __restrict__ partials,
+                                                       unsigned* __restrict__ ticket, double* __restrict__ gosa)
+{
+    __shared__ float ring[4][RSLOT];
+    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * RX + tx;
+    const int i = 1 + blockIdx.x * RX + tx, j = 1 + blockIdx.y * RY + ty;
     const int k0 = 1 + blockIdx.z * kz, k1 = min(k0 + kz, nz + 1);
     const size_t plane = (size_t)px * py;
-    double g = 0.0;
-    if (i <= nx && j <= ny) {
-        size_t c = ((size_t)k0 * py + j) * px + i;
-        float em = __half2float(e[c - plane]), e0 = __half2float(e[c]);
-        for (int k = k0; k < k1; k++) {
-            const float ep = __half2float(e[c + plane]);
-#define EF(di, dj, dk)                                            \
-    ((di) == 0 && (dj) == 0 ? ((dk) < 0 ? em : ((dk) > 0 ? ep : e0)) \
-                            : __half2float(e[c + (ptrdiff_t)(di) + (ptrdiff_t)(dj) * px + (ptrdiff_t)(dk) * (ptrdiff_t)plane]))
-#define CF(n) __half2float(hf.c[n][c])
-            float ne = CF(0) * EF(1, 0, 0) + CF(1) * EF(0, 1, 0) + CF(2) * EF(0, 0, 1);
-            ne += CF(3) * ((EF(1, 1, 0) - EF(1, -1, 0)) - (EF(-1, 1, 0) - EF(-1, -1, 0)));
-            ne += CF(4) * ((EF(0, 1, 1) - EF(0, -1, 1)) - (EF(0, 1, -1) - EF(0, -1, -1)));
-            ne += CF(5) * ((EF(1, 0, 1) - EF(-1, 0, 1)) - (EF(1, 0, -1) - EF(-1, 0, -1)));
-            ne += CF(6) * EF(-1, 0, 0) + CF(7) * EF(0, -1, 0) + CF(8) * EF(0, 0, -1);
-            const float v = e0 + omega * CF(9) * (__ldg(hf.a3 + c) * ne - e0) + __half2float(D[c]);
-#undef EF
-#undef CF
-            en[c] = __float2half_rn(v);
-            const float ss = (v - e0) * inv_omega;
-            g += (double)ss * (double)ss;
-            em = e0;
-            e0 = ep;
-            c += plane;
+    const bool act = i <= nx && j <= ny;
+    // this thread's halo cell (fixed for all planes)
+    int hs = 0, hi = 0, hj = 0;
+    if (t < RHALO) {
+        hs = halo_slot(t);
+        hi = blockIdx.x * RX + hs % RW;  // padded coords: slot (0,0) is (i0-1, j0-1)
+        hj = blockIdx.y * RY + hs / RW;
+    }
+    typedef typename std::conditional<MODE == 0, float, __half>::type L;
+    const L* f = reinterpret_cast<const L*>(pin);
+    float c, h;
+    // planes k0-1, k0, k0+1 into slots, k0+2 in registers
+#pragma unroll
+    for (int d = -1; d <= 1; d++) {
+        ring_fetch<L>(f, k0 + d, i, j, hi, hj, nx, ny, px, plane, t, c, h);
+        ring_store(ring[(k0 + d) & 3], t, tx, ty, hs, c, h);
+    }
+    float nc = 0.0f, nh = 0.0f;
+    if (k0 + 2 <= nz + 1) ring_fetch<L>(f, k0 + 2, i, j, hi, hj, nx, ny, px, plane, t, nc, nh);
+    // coefficients of plane k0
+    const size_t c0 = ((size_t)k0 * py + j) * px + i;
+    float co[12];
+    if (act) {
+        if (MODE == 0) {
+#pragma unroll
+            for (int n = 0; n < 12; n++) co[n] = __ldcs(cf.c[n] + c0);
+        } else {
+#pragma unroll
+            for (int n = 0; n < 10; n++) co[n] = __half2float(__ldcs(hf.c[n] + c0));
+            co[10] = __ldcs(hf.a3 + c0);
+            co[11] = __half2float(__ldcs(D + c0));
         }
+    }
+    __syncthreads();
+    double g = 0.0;
+    for (int k = k0; k < k1; k++) {
+        const size_t cc = ((size_t)k * py + j) * px + i;
+        // prefetch the next plane's coefficients
+        float cn[12];
+        const bool more = k + 1 < k1;
+        if (act && more) {
+            const size_t c1 = cc + plane;
+            if (MODE == 0) {
+#pragma unroll
+                for (int n = 0; n < 12; n++) cn[n] = __ldcs(cf.c[n] + c1);
+            } else {
+#pragma unroll
+                for (int n = 0; n < 10; n++) cn[n] = __half2float(__ldcs(hf.c[n] + c1));
+                cn[10] = __ldcs(hf.a3 + c1);
+                cn[11] = __half2float(__ldcs(D + c1));
+            }
+        }
+        if (act) {
+            const float* sm = ring[(k - 1) & 3];
+            const float* s0 = ring[k & 3];
+            const float* sp = ring[(k + 1) & 3];
+            const int q = (ty + 1) * RW + tx + 1;
+#define RF(di, dj, dk) (((dk) < 0 ? sm : ((dk) > 0 ? sp : s0))[q + (di) + (dj) * RW])
+            if (MODE == 0) {
+                const float s0v = HIMENO_S0(RF, co[0], co[1], co[2], co[4], co[5], co[6], co[7], co[8], co[9], co[11]);
+                const float pc = RF(0, 0, 0);
+                const float ss = fmul(fsub(fmul(s0v, co[3]), pc), co[10]);
+                reinterpret_cast<float*>(pout)[cc] = fadd(pc, fmul(omega, ss));
+                g += (double)ss * (double)ss;
+            } else {
+                // neighbour sum N e (no wrk1), then e' = e + w*bnd*(a3*N e - e) + D
+                float ne = co[0] * RF(1, 0, 0) + co[1] * RF(0, 1, 0) + co[2] * RF(0, 0, 1);
+                ne += co[3] * ((RF(1, 1, 0) - RF(1, -1, 0)) - (RF(-1, 1, 0) - RF(-1, -1, 0)));
+                ne += co[4] * ((RF(0, 1, 1) - RF(0, -1, 1)) - (RF(0, 1, -1) - RF(0, -1, -1)));
+                ne += co[5] * ((RF(1, 0, 1) - RF(-1, 0, 1)) - (RF(1, 0, -1) - RF(-1, 0, -1)));
+                ne += co[6] * RF(-1, 0, 0) + co[7] * RF(0, -1, 0) + co[8] * RF(0, 0, -1);
+                const float e0 = RF(0, 0, 0);
+                const float v = e0 + omega * co[9] * (co[10] * ne - e0) + co[11];
+                reinterpret_cast<__half*>(pout)[cc] = __float2half_rn(v);
+                const float ss = (v - e0) * inv_omega;
+                g += (double)ss * (double)ss;
+            }
+#undef RF
+        }
+        if (more) {
+            // plane k+2 (fetched last iteration) into its slot; its last readers (plane k-1's sweep)
+            // passed the previous barrier
+            ring_store(ring[(k + 2) & 3], t, tx, ty, hs, nc, nh);
+            if (k + 3 <= nz + 1) ring_fetch<L>(f, k + 3, i, j, hi, hj, nx, ny, px, plane, t, nc, nh);
+#pragma unroll
+            for (int n = 0; n < 12; n++) co[n] = cn[n];
+        }
+        __syncthreads();
     }
     if (gosa) gosa_reduce(g, partials, ticket, gosa);
 }
@@ -243,18 +322,19 @@ int appfis_gb_himeno(const float* const* coef, float* p, float* wrk2, int nx, in
     cudaStream_t st = gb::as_stream(stream);
     Coef12 cf;
     for (int n = 0; n < 12; n++) cf.c[n] = coef[n];
-    dim3 blk(HBX, HBY), grd(gb::ceil_div(nx, HBX), gb::ceil_div(ny, HBY), gb::ceil_div(nz, HKZ));
+    dim3 blk(RX, RY), grd(gb::ceil_div(nx, RX), gb::ceil_div(ny, RY), gb::ceil_div(nz, HKZ));
     double* partials = nullptr;
     unsigned* ticket = nullptr;
     if (dev_gosa) GB_TRY(gosa_scratch(grd, &partials, &ticket, st));
     float* buf[2] = {p, wrk2};
+    H10 none = {};
     int ci = 0;
     for (int it = 0; it < iters; it++) {
-        himeno_sweep<HBX, HBY><<<grd, blk, 0, st>>>(cf, buf[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2, HKZ, omega, partials,
-                                                    ticket, dev_gosa ? dev_gosa + it : nullptr);
+        himeno_ring<0><<<grd, blk, 0, st>>>(cf, none, buf[ci], buf[1 - ci], nullptr, nx, ny, nz, pitch, ny + 2, HKZ, omega, 0.0f,
+                                            partials, ticket, dev_gosa ? dev_gosa + it : nullptr);
         ci = 1 - ci;
     }
-    GB_TRY(gb::launched("himeno_sweep"));
+    GB_TRY(gb::launched("himeno_ring<plain>"));
     if (cur_index) *cur_index = ci;
     return APPFIS_GB_OK;
 }
@@ -283,9 +363,10 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     GB_CUDA(cudaMemsetAsync(p_work, 0, sizeof(float) * field, st));
     himeno_half_coef<<<dim3(gb::ceil_div(nx, 128), ny, nz), 128, 0, st>>>(cf, Hc, field, nx, ny, nz, pitch, ny + 2);
     dim3 blk(HBX, HBY), grd(gb::ceil_div(nx, HBX), gb::ceil_div(ny, HBY), gb::ceil_div(nz, HKZ));
-    double* partials = nullptr;
-    unsigned* ticket = nullptr;
-    if (dev_gosa) GB_TRY(gosa_scratch(grd, &partials, &ticket, st));
+    dim3 rblk(RX, RY), rgrd(gb::ceil_div(nx, RX), gb::ceil_div(ny, RY), gb::ceil_div(nz, HKZ));
+    double* rpartials = nullptr;
+    unsigned* rticket = nullptr;
+    if (dev_gosa) GB_TRY(gosa_scratch(rgrd, &rpartials, &rticket, st));
     float* P[2] = {p, p_work};
     int pc = 0, ec = 0;
     // D from the initial P (e = 0), e restarted at 0
@@ -294,8 +375,8 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     ec = 1 - ec;
     const float inv_omega = 1.0f / omega;
     for (int it = 0; it < iters; it++) {
-        himeno_inner<HBX, HBY><<<grd, blk, 0, st>>>(hf, E[ec], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2, HKZ, omega, inv_omega,
-                                                    partials, ticket, dev_gosa ? dev_gosa + it : nullptr);
+        himeno_ring<1><<<rgrd, rblk, 0, st>>>(cf, hf, E[ec], E[1 - ec], Dd, nx, ny, nz, pitch, ny + 2, HKZ, omega, inv_omega,
+                                              rpartials, rticket, dev_gosa ? dev_gosa + it : nullptr);
         ec = 1 - ec;
         if ((it + 1) % period == 0 || it + 1 == iters) {
             himeno_correct<HBX, HBY><<<grd, blk, 0, st>>>(cf, P[pc], E[ec], P[1 - pc], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2,

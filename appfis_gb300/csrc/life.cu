@@ -110,8 +110,8 @@ __device__ __forceinline__ RowU8 finish_row_u8(const RawU8& raw, int x0, int nx,
 }
 
 // Warp tasks: a 512-byte strip (32 lanes x 16 cells) over LIFE_ROWS rows, visited grid-stride by
-// a grid sized to the resident capacity.  The loads of row j+2 (cur) and j+1 (old) are issued
-// before row j is computed, so two rows of loads are in flight per lane.
+// a grid sized to the resident capacity.  The loads of rows j+3 (cur) and j+2 (old) are issued
+// before row j is computed, so three rows of loads are in flight per lane.
 template <int RULE>
 __global__ void __launch_bounds__(256) life_u8_swar(const uint8_t* __restrict__ cur, uint8_t* __restrict__ out,
                                                      int nx, int ny, int strips, int tasks)
@@ -125,21 +125,24 @@ __global__ void __launch_bounds__(256) life_u8_swar(const uint8_t* __restrict__ 
         const int j0 = seg * LIFE_ROWS, j1 = min(j0 + LIFE_ROWS, ny);
         RowU8 up = finish_row_u8(load_raw_u8(cur, nx, j0 == 0 ? ny - 1 : j0 - 1, x0, active, lane), x0, nx, lane);
         RowU8 mid = finish_row_u8(load_raw_u8(cur, nx, j0, x0, active, lane), x0, nx, lane);
-        RawU8 rdn = load_raw_u8(cur, nx, j0 == ny - 1 ? 0 : j0 + 1, x0, active, lane);
-        uint4 o = (RULE == APPFIS_GB_LIFE_REFERENCE && active) ? *reinterpret_cast<const uint4*>(out + (size_t)j0 * nx + x0)
-                                                                : make_uint4(0, 0, 0, 0);
+        // two rows of loads in flight: cur rows j+1, j+2 and old rows j, j+1
+        const RawU8 zero = {make_uint4(0, 0, 0, 0), 0u, 0u};
+        RawU8 r1 = load_raw_u8(cur, nx, j0 + 1 >= ny ? j0 + 1 - ny : j0 + 1, x0, active, lane);
+        RawU8 r2 = j0 + 1 < j1 ? load_raw_u8(cur, nx, j0 + 2 >= ny ? j0 + 2 - ny : j0 + 2, x0, active, lane) : zero;
+        const bool ref = RULE == APPFIS_GB_LIFE_REFERENCE && active;
+        uint4 o0 = ref ? *reinterpret_cast<const uint4*>(out + (size_t)j0 * nx + x0) : make_uint4(0, 0, 0, 0);
+        uint4 o1 = (ref && j0 + 1 < j1) ? *reinterpret_cast<const uint4*>(out + (size_t)(j0 + 1) * nx + x0) : make_uint4(0, 0, 0, 0);
         for (int j = j0; j < j1; j++) {
-            RawU8 rnext = {make_uint4(0, 0, 0, 0), 0u, 0u};
-            uint4 onext = make_uint4(0, 0, 0, 0);
-            if (j + 1 < j1) {  // prefetch (warp-uniform)
-                const int r2 = j + 2 >= ny ? j + 2 - ny : j + 2;
-                rnext = load_raw_u8(cur, nx, r2, x0, active, lane);
-                if (RULE == APPFIS_GB_LIFE_REFERENCE && active)
-                    onext = *reinterpret_cast<const uint4*>(out + (size_t)(j + 1) * nx + x0);
+            RawU8 r3 = zero;
+            uint4 o2 = make_uint4(0, 0, 0, 0);
+            if (j + 2 < j1) {  // prefetch (warp-uniform)
+                const int rr = j + 3 >= ny ? j + 3 - ny : j + 3;
+                r3 = load_raw_u8(cur, nx, rr, x0, active, lane);
+                if (ref) o2 = *reinterpret_cast<const uint4*>(out + (size_t)(j + 2) * nx + x0);
             }
-            const RowU8 dn = finish_row_u8(rdn, x0, nx, lane);
+            const RowU8 dn = finish_row_u8(r1, x0, nx, lane);
             if (active) {
-                const uint32_t ow[4] = {o.x, o.y, o.z, o.w};
+                const uint32_t ow[4] = {o0.x, o0.y, o0.z, o0.w};
                 uint32_t nw[4];
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
@@ -150,8 +153,10 @@ __global__ void __launch_bounds__(256) life_u8_swar(const uint8_t* __restrict__ 
             }
             up = mid;
             mid = dn;
-            rdn = rnext;
-            o = onext;
+            r1 = r2;
+            r2 = r3;
+            o0 = o1;
+            o1 = o2;
         }
     }
 }
@@ -234,6 +239,110 @@ __global__ void __launch_bounds__(256) life_bits_sweep(const uint32_t* __restric
             rdn = rnext;
             o = onext;
         }
+    }
+}
+
+// ------------------------------------------------------------------------------ bit-packed, time-blocked
+// TB_STEPS generations per launch on a tile held in shared memory.  A CTA owns output words
+// [30*tx, 30*tx + 30) x rows [R*ty, R*ty + R) and loads a 32-word x (R + 2*TB_STEPS)-row region
+// around it (periodic wrap at load time, so the region is a consistent periodic window even on
+// the grid's last tiles).  Lane 0 / 31 hold the halo words: their outer bits go stale by one
+// cell per generation, which never reaches the output words for up to 31 generations; rows go
+// stale from the region's top/bottom by one row per generation, which never reaches the R
+// output rows for up to TB_STEPS generations.  Both states (t and t-1) are kept: each
+// generation writes the new state in place over the t-1 plane (new(x) reads only old(x) and
+// the current plane), then the planes swap.  The launch reads two planes and writes two planes
+// (the next launch needs both), so global traffic per generation drops by ~TB_STEPS/1.5.
+constexpr int TB_ROWS = 128;  // output rows per tile
+constexpr int TB_STEPS = 16;  // generations per launch (max)
+constexpr int TB_WARPS = 8;
+constexpr int TB_RR = TB_ROWS + 2 * TB_STEPS;
+
+// Row summary of one word for the bit-sliced neighbour count; lanes 0 / 31 see 0 beyond the tile
+// (their outer bits are the stale halo, never read by output words).
+__device__ __forceinline__ RowBits tile_row(uint32_t w, int lane)
+{
+    uint32_t lw = __shfl_up_sync(FULL, w, 1);
+    uint32_t rw = __shfl_down_sync(FULL, w, 1);
+    if (lane == 0) lw = 0u;
+    if (lane == 31) rw = 0u;
+    const uint32_t L = __funnelshift_l(lw, w, 1), R = __funnelshift_r(w, rw, 1);
+    RowBits r;
+    r.w = w;
+    r.a0 = L ^ w ^ R;
+    r.a1 = (L & w) | (R & (L ^ w));
+    r.h0 = L ^ R;
+    r.h1 = L & R;
+    return r;
+}
+
+template <int RULE>
+__device__ __forceinline__ uint32_t life_combine(const RowBits& up, const RowBits& mid, const RowBits& dn, uint32_t o)
+{
+    const uint32_t t0 = up.a0 ^ mid.h0, c0 = up.a0 & mid.h0;
+    const uint32_t t1 = up.a1 ^ mid.h1 ^ c0, t2 = (up.a1 & mid.h1) | (c0 & (up.a1 ^ mid.h1));
+    const uint32_t r0 = t0 ^ dn.a0, k0 = t0 & dn.a0;
+    const uint32_t r1 = t1 ^ dn.a1 ^ k0, k1 = (t1 & dn.a1) | (k0 & (t1 ^ dn.a1));
+    const uint32_t r2 = t2 ^ k1, r3 = t2 & k1;
+    return rule_bits<RULE>(r0, r1, r2, r3, mid.w, o);
+}
+
+template <int RULE>
+__global__ void __launch_bounds__(TB_WARPS * 32) life_bits_tb(const uint32_t* __restrict__ curG, const uint32_t* __restrict__ oldG,
+                                                               uint32_t* __restrict__ outCur, uint32_t* __restrict__ outOld,
+                                                               int nw, int ny, int tiles_x, int tiles, int steps)
+{
+    __shared__ uint32_t sA[TB_RR][32];
+    __shared__ uint32_t sB[TB_RR][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int tx = tile % tiles_x, ty = tile / tiles_x;
+        int wx = (tx * 30 - 1 + lane) % nw;
+        if (wx < 0) wx += nw;
+        const int row0 = ty * TB_ROWS - TB_STEPS;
+        for (int r = warp; r < TB_RR; r += TB_WARPS) {
+            int gy = (row0 + r) % ny;
+            if (gy < 0) gy += ny;
+            const size_t g = (size_t)gy * nw + wx;
+            sA[r][lane] = __ldg(curG + g);
+            sB[r][lane] = RULE == APPFIS_GB_LIFE_REFERENCE ? __ldg(oldG + g) : 0u;
+        }
+        __syncthreads();
+        uint32_t(*cur)[32] = sA;
+        uint32_t(*old)[32] = sB;
+        for (int t = 1; t <= steps; t++) {
+            // rows valid after generation t: [t, TB_RR - t), split evenly over the warps; each warp
+            // marches its chunk carrying the row summaries (one new row summary per output row)
+            const int lo = t, n = TB_RR - 2 * t, chunk = (n + TB_WARPS - 1) / TB_WARPS;
+            const int r0 = lo + warp * chunk, r1 = min(lo + n, r0 + chunk);
+            if (r0 < r1) {
+                RowBits up = tile_row(cur[r0 - 1][lane], lane);
+                RowBits mid = tile_row(cur[r0][lane], lane);
+                for (int r = r0; r < r1; r++) {
+                    const RowBits dn = tile_row(cur[r + 1][lane], lane);
+                    const uint32_t o = RULE == APPFIS_GB_LIFE_REFERENCE ? old[r][lane] : 0u;
+                    old[r][lane] = life_combine<RULE>(up, mid, dn, o);
+                    up = mid;
+                    mid = dn;
+                }
+            }
+            __syncthreads();
+            uint32_t(*tmp)[32] = cur;
+            cur = old;
+            old = tmp;
+        }
+        const int wout = tx * 30 - 1 + lane;
+        if (lane >= 1 && lane <= 30 && wout < nw) {
+            for (int r = TB_STEPS + warp; r < TB_STEPS + TB_ROWS; r += TB_WARPS) {
+                const int gy = ty * TB_ROWS + (r - TB_STEPS);
+                if (gy < ny) {
+                    const size_t g = (size_t)gy * nw + wout;
+                    outCur[g] = cur[r][lane];
+                    outOld[g] = old[r][lane];
+                }
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -332,19 +441,50 @@ int run_u8(uint8_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStream
     return APPFIS_GB_OK;
 }
 
+// Time-blocked launches for whole blocks of TB_STEPS generations (ping-pong between (a, b) and
+// two workspace planes), single-generation sweeps for the remainder.  The newest state ends in
+// a or b as cur_index says.
 template <int RULE>
 int run_bits(uint32_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStream_t st)
 {
     const int nw = nx / 32;
-    const int strips = (nw + 31) / 32;
-    const int tasks = strips * ((ny + LIFE_ROWS - 1) / LIFE_ROWS);
-    const unsigned grid = resident_grid(life_bits_sweep<RULE>, tasks);
     int ci = 0;
-    for (int g = 0; g < gens; g++) {
-        life_bits_sweep<RULE><<<grid, 256, 0, st>>>(buf[ci], buf[1 - ci], nw, ny, strips, tasks);
-        ci = 1 - ci;
+    const size_t plane = (size_t)nw * ny;
+    if (gens >= TB_STEPS) {
+        void *wc, *wd;
+        GB_TRY(gb::workspace(gb::WS_LIFE_C, sizeof(uint32_t) * plane, &wc));
+        GB_TRY(gb::workspace(gb::WS_LIFE_D, sizeof(uint32_t) * plane, &wd));
+        uint32_t* P[2][2] = {{buf[0], buf[1]}, {(uint32_t*)wc, (uint32_t*)wd}};  // [pair][cur/old]
+        const int tiles_x = (nw + 29) / 30, tiles = tiles_x * ((ny + TB_ROWS - 1) / TB_ROWS);
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, life_bits_tb<RULE>, TB_WARPS * 32, 0) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 4;
+        const int grid = std::max(1, std::min(tiles, per_sm * gb::sm_count()));
+        int pair = 0;
+        int done = 0;
+        for (; done + TB_STEPS <= gens; done += TB_STEPS) {
+            life_bits_tb<RULE><<<grid, TB_WARPS * 32, 0, st>>>(P[pair][0], P[pair][1], P[1 - pair][0], P[1 - pair][1], nw, ny,
+                                                               tiles_x, tiles, TB_STEPS);
+            pair = 1 - pair;
+        }
+        GB_TRY(gb::launched("life_bits_tb"));
+        if (pair == 1) {  // bring the (cur, old) pair back into (a, b)
+            GB_CUDA(cudaMemcpyAsync(buf[0], P[1][0], sizeof(uint32_t) * plane, cudaMemcpyDeviceToDevice, st));
+            GB_CUDA(cudaMemcpyAsync(buf[1], P[1][1], sizeof(uint32_t) * plane, cudaMemcpyDeviceToDevice, st));
+        }
+        gens -= done;
     }
-    GB_TRY(gb::launched("life_bits sweep"));
+    if (gens > 0) {
+        const int strips = (nw + 31) / 32;
+        const int tasks = strips * ((ny + LIFE_ROWS - 1) / LIFE_ROWS);
+        const unsigned grid = resident_grid(life_bits_sweep<RULE>, tasks);
+        for (int g = 0; g < gens; g++) {
+            life_bits_sweep<RULE><<<grid, 256, 0, st>>>(buf[ci], buf[1 - ci], nw, ny, strips, tasks);
+            ci = 1 - ci;
+        }
+        GB_TRY(gb::launched("life_bits sweep"));
+    }
     if (cur_index) *cur_index = ci;
     return APPFIS_GB_OK;
 }

@@ -41,64 +41,90 @@ template <class T, int MODE, int RY>
 __global__ void __launch_bounds__(256) star_r4_sweep(const T* __restrict__ in, T* __restrict__ out, int nx, int ny, int nz,
                                                       int px, int py, int kz, float coeff, StarW wt)
 {
-    constexpr int TY = 8 * RY;
-    constexpr int SW = TX + 2 * R;  // shared tile width
-    __shared__ float tile[(TY + 2 * R) * SW];
+    constexpr int NTY = 8;          // thread rows of the block (32 x 8 threads)
+    constexpr int TY = NTY * RY;    // tile rows: each thread owns RY consecutive rows
+    constexpr int SW = TX + 2 * R;  // shared plane width
+    constexpr int SH = TY + 2 * R;
+    constexpr int NHALO = 8 * TY + 8 * TX;          // x halo (2 sides x 4 x TY) + y halo (2 x 4 x TX)
+    constexpr int HPT = (NHALO + 255) / 256;        // halo values per thread per plane
+    __shared__ float tile[2][SH * SW];
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
     const int x0 = R + blockIdx.x * TX, y0 = R + blockIdx.y * TY;
     const int k0 = R + blockIdx.z * kz, k1 = min(k0 + kz, nz + R);
     const int xe = nx + 2 * R, ye = ny + 2 * R;  // padded extents
     const size_t plane = (size_t)px * py;
-    const int x = x0 + tx;
+    const int x = x0 + tx, yb = y0 + ty * RY;
 
-    float q[RY][2 * R + 1];
-    // queue: z = k0-4 .. k0+3 in slots 0..7; slot 8 filled at the top of each step
+    // halo items of this thread: padded (hx, hy) and shared offset, fixed for all planes
+    int hoff[HPT];
+    size_t hsrc[HPT];
+    bool hok[HPT];
+#pragma unroll
+    for (int h = 0; h < HPT; h++) {
+        const int item = t + 256 * h;
+        int hx = 0, hy = 0;
+        hok[h] = item < NHALO;
+        if (item < 8 * TY) {
+            const int side = item / (4 * TY), rem = item - side * 4 * TY;
+            hx = side ? x0 + TX + (rem & 3) : x0 - R + (rem & 3);
+            hy = y0 + (rem >> 2);
+        } else {
+            const int it2 = item - 8 * TY;
+            const int side = it2 / (4 * TX), rem = it2 - side * 4 * TX;
+            hx = x0 + (rem % TX);
+            hy = side ? y0 + TY + rem / TX : y0 - R + rem / TX;
+        }
+        hoff[h] = (hy - y0 + R) * SW + (hx - x0 + R);
+        hok[h] = hok[h] && hx < xe && hy < ye;
+        hsrc[h] = (size_t)hy * px + hx;
+    }
+
+    float q[RY][2 * R + 1];  // z queue of each owned point: planes k-4 .. k+4
 #pragma unroll
     for (int r = 0; r < RY; r++) {
-        const int y = y0 + ty + 8 * r;
+        const int y = yb + r;
         const bool in_pad = x < xe && y < ye;
 #pragma unroll
         for (int m = 0; m < 2 * R; m++)
             q[r][m] = in_pad ? ld<T>(in + (size_t)(k0 - R + m) * plane + (size_t)y * px + x) : 0.0f;
     }
-    // halo assignment (2 values per thread per plane)
-    const int side = t >> 7, idx = t & 127;
-    const int hx_lr = side ? x0 + TX + (idx & 3) : x0 - R + (idx & 3);  // left/right halo column
-    const int hy_lr = y0 + (idx >> 2);                                   // rows y0 .. y0+31
-    const int hx_tb = x0 + (idx & 31);
-    const int hy_tb = side ? y0 + TY + (idx >> 5) : y0 - R + (idx >> 5);
+    float hv[HPT];
+#pragma unroll
+    for (int h = 0; h < HPT; h++) hv[h] = hok[h] ? ld<T>(in + (size_t)k0 * plane + hsrc[h]) : 0.0f;
+    // plane k0 into tile[0]
+#pragma unroll
+    for (int r = 0; r < RY; r++) tile[0][(ty * RY + r + R) * SW + tx + R] = q[r][R];
+#pragma unroll
+    for (int h = 0; h < HPT; h++)
+        if (t + 256 * h < NHALO) tile[0][hoff[h]] = hv[h];
+    __syncthreads();
 
     for (int k = k0; k < k1; k++) {
+        const int b = (k - k0) & 1;
+        // prefetch: plane k+4 for the queues, plane k+1 for the halo
 #pragma unroll
         for (int r = 0; r < RY; r++) {
-            const int y = y0 + ty + 8 * r;
-            const bool in_pad = x < xe && y < ye;
-            q[r][2 * R] = in_pad ? ld<T>(in + (size_t)(k + R) * plane + (size_t)y * px + x) : 0.0f;
+            const int y = yb + r;
+            q[r][2 * R] = (x < xe && y < ye) ? ld<T>(in + (size_t)(k + R) * plane + (size_t)y * px + x) : 0.0f;
         }
-        __syncthreads();  // previous plane's tile reads are done
+        if (k + 1 < k1) {
 #pragma unroll
-        for (int r = 0; r < RY; r++) tile[(ty + 8 * r + R) * SW + tx + R] = q[r][R];
-        const size_t pk = (size_t)k * plane;
-        for (int h = hy_lr; h < y0 + TY; h += 32) {  // TY may exceed 32: cover every row
-            float v = (hx_lr < xe && h < ye) ? ld<T>(in + pk + (size_t)h * px + hx_lr) : 0.0f;
-            tile[(h - y0 + R) * SW + (hx_lr - x0 + R)] = v;
+            for (int h = 0; h < HPT; h++) hv[h] = hok[h] ? ld<T>(in + (size_t)(k + 1) * plane + hsrc[h]) : 0.0f;
         }
-        {
-            float v = (hx_tb < xe && hy_tb < ye) ? ld<T>(in + pk + (size_t)hy_tb * px + hx_tb) : 0.0f;
-            tile[(hy_tb - y0 + R) * SW + (hx_tb - x0 + R)] = v;
-        }
-        __syncthreads();
+        const float* s = tile[b];
+        float col[RY + 2 * R];  // the thread's column in this plane, rows yb-4 .. yb+RY+3
+#pragma unroll
+        for (int m = 0; m < RY + 2 * R; m++) col[m] = s[(ty * RY + m) * SW + tx + R];
 #pragma unroll
         for (int r = 0; r < RY; r++) {
-            const int yy = ty + 8 * r + R, xx = tx + R;
-            const float* s = tile + yy * SW + xx;
+            const float* row = s + (ty * RY + r + R) * SW + tx + R;
             float v;
             if (MODE == 0) {
                 v = q[r][R];
 #pragma unroll
                 for (int a = 1; a <= R; a++) {
-                    const float sx = __fadd_rn(s[-a], s[a]);
-                    const float sy = __fadd_rn(s[-a * SW], s[a * SW]);
+                    const float sx = __fadd_rn(row[-a], row[a]);
+                    const float sy = __fadd_rn(col[r + R - a], col[r + R + a]);
                     const float sz = __fadd_rn(q[r][R - a], q[r][R + a]);
                     v = __fadd_rn(v, __fadd_rn(__fadd_rn(sx, sy), sz));
                 }
@@ -107,15 +133,166 @@ __global__ void __launch_bounds__(256) star_r4_sweep(const T* __restrict__ in, T
                 v = wt.w[0] * q[r][R];
 #pragma unroll
                 for (int a = 1; a <= R; a++)
-                    v += wt.w[a] * (((s[-a] + s[a]) + (s[-a * SW] + s[a * SW])) + (q[r][R - a] + q[r][R + a]));
+                    v += wt.w[a] * (((row[-a] + row[a]) + (col[r + R - a] + col[r + R + a])) + (q[r][R - a] + q[r][R + a]));
             }
-            const int y = y0 + ty + 8 * r;
+            const int y = yb + r;
             if (x < nx + R && y < ny + R) st<T>(out + (size_t)k * plane + (size_t)y * px + x, v);
         }
 #pragma unroll
         for (int r = 0; r < RY; r++)
 #pragma unroll
             for (int m = 0; m < 2 * R; m++) q[r][m] = q[r][m + 1];
+        if (k + 1 < k1) {  // plane k+1 into the other buffer (its last readers passed the previous barrier)
+            float* d = tile[1 - b];
+#pragma unroll
+            for (int r = 0; r < RY; r++) d[(ty * RY + r + R) * SW + tx + R] = q[r][R];
+#pragma unroll
+            for (int h = 0; h < HPT; h++)
+                if (t + 256 * h < NHALO) d[hoff[h]] = hv[h];
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- vectorised form
+// Each thread owns 4 consecutive x points of one row (16 x 16 threads = a 64 x 16 tile), so a
+// row of the shared plane is read as float4 (x-window x-4 .. x+7 = three 16-byte reads) and the
+// y-window as one float4 per row.  The z queue holds 9 float4 planes; the plane loop is unrolled
+// by 9 so the queue rotates by register renaming instead of moves.  Requires 16-byte aligned
+// rows: pitch % 4 == 0 (FP32) / pitch % 8 == 0 (FP16, 8-byte half4 loads) and an aligned base.
+constexpr int VX = 4, VTX = 64, VTY = 16;
+constexpr int VSW = VTX + 2 * R, VSH = VTY + 2 * R;
+
+template <class T> struct Vec4;
+template <> struct Vec4<float> {
+    static __device__ __forceinline__ float4 ld(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+    static __device__ __forceinline__ void st(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+};
+template <> struct Vec4<__half> {
+    static __device__ __forceinline__ float4 ld(const __half* p)
+    {
+        const uint2 u = __ldg(reinterpret_cast<const uint2*>(p));
+        const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+        const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+        return make_float4(a.x, a.y, b.x, b.y);
+    }
+    static __device__ __forceinline__ void st(__half* p, float4 v)
+    {
+        const __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
+        uint2 u;
+        u.x = *reinterpret_cast<const uint32_t*>(&a);
+        u.y = *reinterpret_cast<const uint32_t*>(&b);
+        *reinterpret_cast<uint2*>(p) = u;
+    }
+};
+
+__device__ __forceinline__ float f4(const float4& v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w)); }
+
+template <class T, int MODE>
+__global__ void __launch_bounds__(256) star_r4_vec(const T* __restrict__ in, T* __restrict__ out, int nx, int ny, int nz, int px,
+                                                    int py, int kz, float coeff, StarW wt)
+{
+    __shared__ __align__(16) float tile[2][VSH * VSW];
+    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * 16 + tx;
+    const int x0 = R + blockIdx.x * VTX, y0 = R + blockIdx.y * VTY;
+    const int k0 = R + blockIdx.z * kz, k1 = min(k0 + kz, nz + R);
+    const int xe = nx + 2 * R, ye = ny + 2 * R;
+    const size_t plane = (size_t)px * py;
+    const int x = x0 + VX * tx, y = y0 + ty;
+    const bool inpad = x < xe && y < ye;  // x % 4 == 0 and xe % 4 == 0 when pitch is aligned: all 4 in or out
+    const size_t own = (size_t)y * px + x;
+    // halo vectors of this thread: y halo = 8 rows x 16 vectors (items 0..127); x halo = 2 sides x 16
+    // rows (items 128..159); 160 items over 256 threads
+    const bool has_h = t < 160;
+    int hoff = 0;
+    size_t hsrc = 0;
+    bool hok = false;
+    if (has_h) {
+        int hx, hy;
+        if (t < 128) {
+            const int row = t >> 4;  // 0..7: rows y0-4..y0-1, y0+VTY..y0+VTY+3
+            hy = row < 4 ? y0 - R + row : y0 + VTY + (row - 4);
+            hx = x0 + VX * (t & 15);
+        } else {
+            const int it = t - 128, side = it >> 4;
+            hy = y0 + (it & 15);
+            hx = side ? x0 + VTX : x0 - R;
+        }
+        hoff = (hy - y0 + R) * VSW + (hx - x0 + R);
+        hok = hx < xe && hy < ye;
+        hsrc = (size_t)hy * px + hx;
+    }
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 q[9];
+#pragma unroll
+    for (int m = 0; m < 8; m++) q[m] = inpad ? Vec4<T>::ld(in + (size_t)(k0 - R + m) * plane + own) : z4;
+    float4 hv = (has_h && hok) ? Vec4<T>::ld(in + (size_t)k0 * plane + hsrc) : z4;
+    {
+        float* d = tile[0];
+        *reinterpret_cast<float4*>(d + (ty + R) * VSW + R + VX * tx) = q[R];
+        if (has_h) *reinterpret_cast<float4*>(d + hoff) = hv;
+    }
+    __syncthreads();
+    for (int kb = k0; kb < k1; kb += 9) {
+#pragma unroll
+        for (int P = 0; P < 9; P++) {
+            const int k = kb + P;
+            if (k < k1) {
+                const int b = (k - k0) & 1;
+                q[(P + 8) % 9] = inpad ? Vec4<T>::ld(in + (size_t)(k + R) * plane + own) : z4;
+                const bool more = k + 1 < k1;
+                if (more) hv = (has_h && hok) ? Vec4<T>::ld(in + (size_t)(k + 1) * plane + hsrc) : z4;
+                const float* s = tile[b];
+                const float* rowp = s + (ty + R) * VSW + R + VX * tx;  // this thread's 4 points
+                const float4 xl = *reinterpret_cast<const float4*>(rowp - 4);
+                const float4 xc = *reinterpret_cast<const float4*>(rowp);
+                const float4 xr = *reinterpret_cast<const float4*>(rowp + 4);
+                float4 ym[R], yp[R];
+#pragma unroll
+                for (int a = 1; a <= R; a++) {
+                    ym[a - 1] = *reinterpret_cast<const float4*>(rowp - a * VSW);
+                    yp[a - 1] = *reinterpret_cast<const float4*>(rowp + a * VSW);
+                }
+                const float xw[12] = {xl.x, xl.y, xl.z, xl.w, xc.x, xc.y, xc.z, xc.w, xr.x, xr.y, xr.z, xr.w};
+                float res[4];
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const float cen = f4(q[(P + 4) % 9], c);
+                    float v;
+                    if (MODE == 0) {
+                        v = cen;
+#pragma unroll
+                        for (int a = 1; a <= R; a++) {
+                            const float sx = __fadd_rn(xw[4 + c - a], xw[4 + c + a]);
+                            const float sy = __fadd_rn(f4(ym[a - 1], c), f4(yp[a - 1], c));
+                            const float sz = __fadd_rn(f4(q[(P + 4 - a) % 9], c), f4(q[(P + 4 + a) % 9], c));
+                            v = __fadd_rn(v, __fadd_rn(__fadd_rn(sx, sy), sz));
+                        }
+                        v = __fmul_rn(v, coeff);
+                    } else {
+                        v = wt.w[0] * cen;
+#pragma unroll
+                        for (int a = 1; a <= R; a++)
+                            v += wt.w[a] * (((xw[4 + c - a] + xw[4 + c + a]) + (f4(ym[a - 1], c) + f4(yp[a - 1], c))) +
+                                            (f4(q[(P + 4 - a) % 9], c) + f4(q[(P + 4 + a) % 9], c)));
+                    }
+                    res[c] = v;
+                }
+                if (x < nx + R && y < ny + R) {
+                    if (x + VX <= nx + R) {
+                        Vec4<T>::st(out + (size_t)k * plane + own, make_float4(res[0], res[1], res[2], res[3]));
+                    } else {  // ragged last vector of a row: only the interior lanes
+                        for (int c = 0; c < VX && x + c < nx + R; c++) st<T>(out + (size_t)k * plane + own + c, res[c]);
+                    }
+                }
+                if (more) {
+                    float* d = tile[1 - b];
+                    *reinterpret_cast<float4*>(d + (ty + R) * VSW + R + VX * tx) = q[(P + 5) % 9];
+                    if (has_h) *reinterpret_cast<float4*>(d + hoff) = hv;
+                }
+                __syncthreads();
+            }
+        }
     }
 }
 
@@ -123,6 +300,7 @@ template <class T, int MODE, int RY>
 void launch_star(const T* in, T* out, int nx, int ny, int nz, int px, int kz, float coeff, StarW w, cudaStream_t st)
 {
     dim3 blk(TX, 8), grd(gb::ceil_div(nx, TX), gb::ceil_div(ny, 8 * RY), gb::ceil_div(nz, kz));
+    static_assert(RY >= 1, "rows per thread");
     star_r4_sweep<T, MODE, RY><<<grd, blk, 0, st>>>(in, out, nx, ny, nz, px, ny + 2 * R, kz, coeff, w);
 }
 
@@ -134,9 +312,16 @@ int run_star(T* a, T* b, int nx, int ny, int nz, int pitch, int iters, int mode,
     if (w5)
         for (int n = 0; n < 5; n++) w.w[n] = w5[n];
     T* buf[2] = {a, b};
+    const int align = sizeof(T) == 4 ? 4 : 4;  // elements per vector: rows and base must allow 4-wide access
+    const bool vec = ry == 0 && pitch % align == 0 && ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) %
+                                                          (sizeof(T) * 4)) == 0;
     int ci = 0;
     for (int it = 0; it < iters; it++) {
-        if (mode == 0) {
+        if (vec) {
+            dim3 blk(16, 16), grd(gb::ceil_div(nx, VTX), gb::ceil_div(ny, VTY), gb::ceil_div(nz, kz));
+            if (mode == 0) star_r4_vec<T, 0><<<grd, blk, 0, st>>>(buf[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2 * R, kz, coeff, w);
+            else star_r4_vec<T, 1><<<grd, blk, 0, st>>>(buf[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2 * R, kz, coeff, w);
+        } else if (mode == 0) {
             if (ry == 2) launch_star<T, 0, 2>(buf[ci], buf[1 - ci], nx, ny, nz, pitch, kz, coeff, w, st);
             else launch_star<T, 0, 4>(buf[ci], buf[1 - ci], nx, ny, nz, pitch, kz, coeff, w, st);
         } else {
@@ -145,7 +330,7 @@ int run_star(T* a, T* b, int nx, int ny, int nz, int pitch, int iters, int mode,
         }
         ci = 1 - ci;
     }
-    GB_TRY(gb::launched("star_r4_sweep"));
+    GB_TRY(gb::launched("star_r4 sweep"));
     if (cur_index) *cur_index = ci;
     return APPFIS_GB_OK;
 }
@@ -162,9 +347,9 @@ int appfis_gb_star_r4(void* a, void* b, int dtype, int nx, int ny, int nz, int p
     if (mode != 0 && mode != 1) return gb::fail(APPFIS_GB_EINVAL, "star_r4: mode %d", mode);
     if (mode == 1 && !weights) return gb::fail(APPFIS_GB_EINVAL, "star_r4: weighted mode needs 5 weights");
     if (iters < 0) return gb::fail(APPFIS_GB_EINVAL, "star_r4: negative iteration count");
-    const int ry = tile_rows <= 0 ? 4 : tile_rows;
-    if (ry != 2 && ry != 4) return gb::fail(APPFIS_GB_EINVAL, "star_r4: tile_rows must be 2 or 4");
-    const int kz = zchunk <= 0 ? 64 : zchunk;
+    const int ry = tile_rows < 0 ? 0 : tile_rows;  // 0: vectorised tile when the rows are 16-byte aligned
+    if (ry != 0 && ry != 2 && ry != 4) return gb::fail(APPFIS_GB_EINVAL, "star_r4: tile_rows must be 0, 2 or 4");
+    const int kz = zchunk <= 0 ? 32 : zchunk;
     cudaStream_t st = gb::as_stream(stream);
     if (dtype == APPFIS_GB_F32)
         return run_star<float>((float*)a, (float*)b, nx, ny, nz, pitch, iters, mode, coeff, weights, ry, kz, cur_index, st);

@@ -498,9 +498,7 @@ def bench_flood(torch, gb, W, dev, sp):
     assert int(status.item()) == 0
     cells = np.array([d[0].size for d in doms], dtype=np.int64)
     cell_steps = float((cells * st).sum())
-    ms_s = _time(torch, sp, one_by_one, reps=1)
-    setup_ms = _time(torch, sp, setup, reps=1)
-    # mass: FP64 sum of h before / after
+    # mass: FP64 sum of h before / after the batched run
     m0 = [float(h.sum().item()) for _, h in inter]
     m1 = []
     for k in range(nd):
@@ -508,6 +506,8 @@ def bench_flood(torch, gb, W, dev, sp):
         ny, nx = doms[k][0].shape
         m1.append(float(bufs[k][b][1:ny + 1, 1:nx + 1].double().sum().item()))
     drift = max(abs(a - b) / a for a, b in zip(m0, m1))
+    ms_s = _time(torch, sp, one_by_one, reps=1)
+    setup_ms = _time(torch, sp, setup, reps=1)
     return {"workload": "flood model, 32 domains (sides 512-3072, %.1f M cells), fractal DEM, to t = 600 s" % (cells.sum() / 1e6),
             "batched_fp32": {"glups": cell_steps / ((ms_b - setup_ms) * 1e-3) / 1e9, "ms": ms_b - setup_ms,
                              "steps_min": int(st.min()), "steps_max": int(st.max()), "cell_steps": cell_steps,
@@ -516,15 +516,68 @@ def bench_flood(torch, gb, W, dev, sp):
             "batched_speedup": (ms_s - setup_ms) / (ms_b - setup_ms)}
 
 
+def profile_small(name, torch, gb, W, dev, sp):
+    """A few launches of one workload's kernels at the benchmark size (no timing)."""
+    ci = ctypes.c_int(0)
+    if name == "heat":
+        c = W.HEAT2D
+        f = torch.from_numpy(W.heat2d_padded(c["nx"], c["ny"], c["top"], c["seed"])).to(dev)
+        a, b = f.clone(), f.clone()
+        gb.call("appfis_gb_heat2d", a.data_ptr(), b.data_ptr(), c["nx"], c["ny"], c["nx"] + 2, 16, c["r"], c["r"],
+                ctypes.byref(ci), sp.cuda_stream)
+    elif name == "himeno":
+        c = W.HIMENO
+        nx, ny, nz = c["nx"], c["ny"], c["nz"]
+        coef = torch.from_numpy(W.himeno_coef(nx, ny, nz)).to(dev)
+        p0 = torch.from_numpy(W.himeno_p(nx, ny, nz)).to(dev)
+        ptrs = (ctypes.c_void_p * 12)(*[coef[k].data_ptr() for k in range(12)])
+        pa, pb = p0.clone(), p0.clone()
+        half = torch.empty(13 * p0.numel(), dtype=torch.float16, device=dev)
+        gosa = torch.zeros(8, dtype=torch.float64, device=dev)
+        gb.call("appfis_gb_himeno", ptrs, pa.data_ptr(), pb.data_ptr(), nx, ny, nz, nx + 2, 5, c["omega"], gosa.data_ptr(),
+                ctypes.byref(ci), sp.cuda_stream)
+        gb.call("appfis_gb_himeno_mixed", ptrs, pa.data_ptr(), pb.data_ptr(), half.data_ptr(), nx, ny, nz, nx + 2, 5, 20,
+                c["omega"], gosa.data_ptr(), ctypes.byref(ci), sp.cuda_stream)
+    elif name == "fdtd":
+        c = W.FDTD
+        nx, ny, nz = c["nx"], c["ny"], c["nz"]
+        w = (ctypes.c_float * 5)(*W.fdtd_weights())
+        f = torch.from_numpy(W.fdtd_padded(nx, ny, nz, c["seed"])).to(dev)
+        a, b = f.clone(), f.clone()
+        gb.call("appfis_gb_star_r4", a.data_ptr(), b.data_ptr(), 0, nx, ny, nz, nx + 8, 5, 1, 0.0, w, 0, 0, ctypes.byref(ci),
+                sp.cuda_stream)
+        h = f.half()
+        ha, hb = h.clone(), h.clone()
+        gb.call("appfis_gb_star_r4", ha.data_ptr(), hb.data_ptr(), 3, nx, ny, nz, nx + 8, 5, 1, 0.0, w, 0, 0, ctypes.byref(ci),
+                sp.cuda_stream)
+
+
 def profile_case(name, local):
-    """Short fixed launch sequences for ncu captures: 16384^2 GameOfLife, 20 bit-packed sweeps
-    then 20 u8 sweeps (kernel order: life_pack, life_bits_sweep x20, life_u8_swar x20)."""
+    """Short fixed launch sequences for ncu captures.
+    life:   16384^2 GameOfLife, 20 bit-packed generations (one life_bits_tb launch of 16 + 4
+            life_bits_sweep) then 20 u8 sweeps (life_u8_swar)
+    himeno: 257x257x513, 5 plain sweeps (himeno_sweep), 5 mixed sweeps (himeno_inner, himeno_correct)
+    fdtd:   512^3, 5 FP32 steps then 5 FP16 steps (star_r4_sweep)
+    heat:   1024^2, 16 iterations (2 heat2d_blocked launches)
+    flood:  4 domains of 512^2, 10 steps (one flood_persistent launch)"""
     import torch
 
     import appfis_gb300 as gb
     from appfis_gb300 import workloads as W
 
     dev = torch.device("cuda", local)
+    sp = torch.cuda.current_stream(dev)
+    if name != "life":
+        fn = {"himeno": bench_himeno, "fdtd": bench_fdtd, "heat": bench_heat}.get(name)
+        if name == "flood":
+            from appfis_gb300 import _lib
+            doms = [W.triton_domain(512, 512, 4242 + k) for k in range(4)]
+            _lib.flood_job(doms, 10.0, 0.5, 1e-3, 0.035, 600.0, 600.0, 1.0, max_steps=10, dtype=_lib.F32)
+        else:
+            profile_small(name, torch, gb, W, dev, sp)
+        torch.cuda.synchronize(dev)
+        print("profile case %s done" % name)
+        return
     cells = torch.from_numpy(W.gol_cells(GOL_NX, GOL_NY, GOL_P, GOL_SEED)).to(dev).view(-1)
     N = GOL_NX * GOL_NY
     wa = torch.empty(N // 32, dtype=torch.int32, device=dev)
@@ -548,7 +601,7 @@ def main():
     ap.add_argument("--ref-gens", type=int, default=8, help="generations per CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-apps", action="store_true", help="skip the per-workload measurements")
-    ap.add_argument("--profile-case", choices=["life"], default=None,
+    ap.add_argument("--profile-case", choices=["life", "himeno", "fdtd", "heat", "flood"], default=None,
                     help="launch a short fixed sequence of the named workload's kernels (for ncu), no timing")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

@@ -40,7 +40,10 @@ def test_golden_reference_form(gb, torch_cuda, f):
 
 @pytest.mark.parametrize("nx,ny,nz,iters,ry,kz,pitch", [(1, 1, 1, 2, 0, 0, None), (37, 29, 11, 3, 4, 0, None),
                                                         (64, 70, 33, 2, 2, 16, 80), (33, 17, 130, 2, 4, 64, None),
-                                                        (100, 3, 5, 4, 2, 3, 112)])
+                                                        (100, 3, 5, 4, 2, 3, 112),
+                                                        # vectorised tile (16-byte rows): aligned, ragged x, ragged y/z
+                                                        (64, 70, 33, 2, 0, 16, 72), (37, 29, 11, 3, 0, 0, 48),
+                                                        (130, 17, 21, 2, 0, 8, 140), (4, 1, 2, 3, 0, 0, 12)])
 def test_reference_form_vs_oracle(gb, torch_cuda, nx, ny, nz, iters, ry, kz, pitch):
     f = W.fdtd_padded(nx, ny, nz, nx * ny + nz)
     out = run(gb, torch_cuda, f, iters, 0, 0.1, pitch=pitch, ry=ry, kz=kz)
@@ -56,6 +59,15 @@ def test_weighted_form_vs_oracle(gb, torch_cuda):
     assert np.abs(out - ref32).max() < 1e-5
     assert np.abs(out - ref64).max() < 1e-5
     assert np.all(out[:4] == 0) and np.all(out[..., :4] == 0)  # halo untouched
+
+
+@pytest.mark.parametrize("pitch,ry", [(None, 2), (72, 0)])
+def test_fp16_both_tiles_agree(gb, torch_cuda, pitch, ry):
+    w = W.fdtd_weights()
+    f = W.fdtd_padded(64, 40, 24, 13)
+    a = run(gb, torch_cuda, f, 6, 1, weights=w, dtype="f16", pitch=pitch, ry=ry)
+    ref64 = O.star_r4(f.astype(np.float64), 6, weights=w, dtype=np.float64)
+    assert np.abs(a - ref64).max() < 2e-3
 
 
 def test_fp16_storage_error(gb, torch_cuda):
