@@ -36,6 +36,23 @@ GOL_P = 0.3
 WORKLOAD = "GameOfLife 16384x16384 u8 cells, periodic, Bernoulli(0.3) seed 42, 2000 generations, reference rule"
 
 
+TB_GENS = 16  # generations per time-blocked bit-packed launch (life.cu TB_STEPS)
+
+
+def profiled_traffic(kernel):
+    """DRAM bytes (read + write) per launch of `kernel` from its ncu summary under profiles/
+    (a line `traffic_bytes_per_launch: <kernel> <bytes>`), or None."""
+    import glob
+    import re
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        with open(path) as f:
+            for line in f:
+                m = re.search(r"traffic_bytes_per_launch:\s*%s\s+([0-9.eE+]+)" % re.escape(kernel), line)
+                if m:
+                    return float(m.group(1))
+    return None
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -249,8 +266,19 @@ def run_ours(args, rank, world, local):
         ms = max_over_ranks(e0.elapsed_time(e1), world) / k
         return ms, (sampler.summary() if sampler else None)
 
-    # headline: bit-packed form, inputs resident in HBM
-    ms_bits, clocks = timed(step_bits, args.steps, args.warmup, sample_clocks=True)
+    # headline: bit-packed form, inputs resident in HBM; the step (pack, 125 time-blocked launches,
+    # population) is replayed from a CUDA graph captured once
+    def step_bits_cur():
+        s_ = torch.cuda.current_stream(dev).cuda_stream
+        gb.call("appfis_gb_life_pack", d_cells.data_ptr(), wa.data_ptr(), GOL_NX, GOL_NY, s_)
+        wb.zero_()
+        gb.call("appfis_gb_life_bits", wa.data_ptr(), wb.data_ptr(), GOL_NX, GOL_NY, gens, 0, ctypes.byref(ci), s_)
+        latest = wa if ci.value == 0 else wb
+        gb.call("appfis_gb_life_population_bits", latest.data_ptr(), nw, cnt.data_ptr(), s_)
+
+    replay_bits = graph_of(torch, step_bits_cur)
+    ms_stream_bits, _ = timed(step_bits, args.steps, args.warmup)
+    ms_bits, clocks = timed(replay_bits, args.steps, args.warmup, sample_clocks=True)
     population = int(cnt.item())
     value = N * gens / (ms_bits * 1e-3) / 1e9 * world
 
@@ -264,10 +292,13 @@ def run_ours(args, rank, world, local):
         torch.cuda.synchronize(dev)
         return e0.elapsed_time(e1) / g
 
+    # the dominant kernel is life_bits_tb: one launch advances the whole grid by TB_GENS generations;
+    # its algorithmic bytes are the compulsory per-sweep bytes (cur + old read, new written: 3 bits
+    # per cell) times the generations it covers, so time blocking can read above 1.0
     gb.call("appfis_gb_life_pack", d_cells.data_ptr(), wa.data_ptr(), GOL_NX, GOL_NY, sp)
-    kernel_avg("appfis_gb_life_bits", wa, wb, 20)
-    bits_ms = kernel_avg("appfis_gb_life_bits", wa, wb, 400)
-    bits_bytes = N * 3 / 8  # read cur + read old + write new, 1 bit each
+    kernel_avg("appfis_gb_life_bits", wa, wb, 20 * TB_GENS)
+    bits_ms = kernel_avg("appfis_gb_life_bits", wa, wb, 25 * TB_GENS) * TB_GENS  # per launch
+    bits_bytes = N * 3 / 8 * TB_GENS
     bits_achieved = bits_bytes / (bits_ms * 1e-3) / 1e9
 
     # u8 form (the byte-per-cell reference layout)
@@ -301,16 +332,18 @@ def run_ours(args, rank, world, local):
         "metric": METRIC, "value": value, "unit": "GLUP/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_bits, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": "bit-packed (32 cells/word), states identical to u8",
+        "config": {"workload": WORKLOAD, "form": "bit-packed (32 cells/word), states identical to u8; step replayed "
+                   "from a CUDA graph (stream launches: %.3f ms)" % ms_stream_bits,
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "each step starts from the 268 MB u8 grid (larger than L2); the packed state (67 MB for "
                          "both buffers) stays L2-resident across generations within a step",
                    "population": population},
         "e2e": {"value": e2e_value, "unit": "GLUP/s", "h2d_bytes_per_step": N, "d2h_bytes_per_step": N + 8,
                 "ms_per_step": e2e_s * 1e3},
-        "gpu_launches": args.steps * (gens + 2),
+        "gpu_launches": args.steps * (gens // 16 + gens % 16 + 2),  # pack, time-blocked sweeps, remainder, population
         "roofline": {"bound": "hbm", "achieved": bits_achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": bits_achieved / hbm_peak, "traffic": None, "kernel": "life_bits_sweep",
+                     "frac": bits_achieved / hbm_peak, "traffic": profiled_traffic("life_bits_tb"),
+                     "kernel": "life_bits_tb", "generations_per_launch": TB_GENS,
                      "algorithmic_bytes_per_launch": bits_bytes, "avg_launch_ms": bits_ms,
                      "peak_source": peak_kind},
         "forms": {
@@ -358,29 +391,63 @@ def _time(torch, stream, fn, reps=2, warmup=1):
     return e0.elapsed_time(e1) / reps  # ms
 
 
+def graph_of(torch, fn):
+    """Captures fn() (library calls on the current stream) into a CUDA graph; returns replay()."""
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        fn()  # warm: workspace allocated outside the capture
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g):
+        fn()
+    return g.replay
+
+
 def bench_heat(torch, gb, W, dev, sp, hbm):
     c = W.HEAT2D
     nx, ny, it = c["nx"], c["ny"], c["iters"]
     f = torch.from_numpy(W.heat2d_padded(nx, ny, c["top"], c["seed"])).to(dev)
     a, b = f.clone(), f.clone()
     ci = ctypes.c_int(0)
-    ms = _time(torch, sp, lambda: gb.call("appfis_gb_heat2d", a.data_ptr(), b.data_ptr(), nx, ny, nx + 2, it, c["r"], c["r"],
-                                          ctypes.byref(ci), sp.cuda_stream))
+
+    def run():
+        gb.call("appfis_gb_heat2d", a.data_ptr(), b.data_ptr(), nx, ny, nx + 2, it, c["r"], c["r"], ctypes.byref(ci),
+                torch.cuda.current_stream().cuda_stream)
+
+    ms = _time(torch, sp, run)
+    ms_g = _time(torch, sp, graph_of(torch, run))
     lups = nx * ny * it
-    gbs = lups * 8 / (ms * 1e-3) / 1e9
-    return {"workload": "heat2d 1024^2 FP32, 1000 iterations, Dirichlet", "glups": lups / (ms * 1e-3) / 1e9, "ms": ms,
-            "bytes_per_lup": 8, "effective_gbs": gbs, "frac_of_hbm": gbs / hbm,
-            "note": "8.4 MB working set is L2-resident; 8 sweeps per launch in shared memory; HBM fraction is nominal",
+    best = min(ms, ms_g)
+    gbs = lups * 8 / (best * 1e-3) / 1e9
+    return {"workload": "heat2d 1024^2 FP32, 1000 iterations, Dirichlet", "glups": lups / (best * 1e-3) / 1e9, "ms": best,
+            "ms_stream_launches": ms, "ms_cuda_graph": ms_g, "bytes_per_lup": 8, "effective_gbs": gbs, "frac_of_hbm": gbs / hbm,
+            "note": "8.4 MB working set is L2-resident; 8 sweeps per launch in shared memory (125 launches, replayed "
+                    "from a CUDA graph); HBM fraction is nominal",
             "form": "plain FP32 (bit-identical to the reference CPU path)"}
 
 
+def _pad_x(t, pitch):
+    """Copy of t with its last (x) axis padded with zeros to `pitch` elements."""
+    out = t.new_zeros(tuple(t.shape[:-1]) + (pitch,))
+    out[..., : t.shape[-1]] = t
+    return out
+
+
 def bench_himeno(torch, gb, W, dev, sp, hbm):
+    """Both forms on rows padded to 264 elements (16-byte aligned FP16 and FP32 rows: the
+    TMA-staged kernels), plus one-sweep times of the register-prefetch kernels on the dense
+    259-element rows for comparison."""
     c = W.HIMENO
     nx, ny, nz, it, om = c["nx"], c["ny"], c["nz"], c["iters"], c["omega"]
-    coef = torch.from_numpy(W.himeno_coef(nx, ny, nz)).to(dev)
-    p0 = torch.from_numpy(W.himeno_p(nx, ny, nz)).to(dev)
+    pitch = (nx + 2 + 7) // 8 * 8
+    coef_d = torch.from_numpy(W.himeno_coef(nx, ny, nz)).to(dev)
+    p0_d = torch.from_numpy(W.himeno_p(nx, ny, nz)).to(dev)
+    coef = _pad_x(coef_d, pitch)
+    p0 = _pad_x(p0_d, pitch)
     ptrs = (ctypes.c_void_p * 12)(*[coef[k].data_ptr() for k in range(12)])
-    field = (nx + 2) * (ny + 2) * (nz + 2)
+    field = pitch * (ny + 2) * (nz + 2)
     pa, pb = p0.clone(), p0.clone()
     half = torch.empty(13 * field, dtype=torch.float16, device=dev)
     gosa = torch.zeros(it, dtype=torch.float64, device=dev)
@@ -389,12 +456,12 @@ def bench_himeno(torch, gb, W, dev, sp, hbm):
 
     def plain():
         pa.copy_(p0)
-        gb.call("appfis_gb_himeno", ptrs, pa.data_ptr(), pb.data_ptr(), nx, ny, nz, nx + 2, it, om, gosa.data_ptr(),
+        gb.call("appfis_gb_himeno", ptrs, pa.data_ptr(), pb.data_ptr(), nx, ny, nz, pitch, it, om, gosa.data_ptr(),
                 ctypes.byref(ci), sp.cuda_stream)
 
     def mixed():
         pa.copy_(p0)
-        gb.call("appfis_gb_himeno_mixed", ptrs, pa.data_ptr(), pb.data_ptr(), half.data_ptr(), nx, ny, nz, nx + 2, it, 20, om,
+        gb.call("appfis_gb_himeno_mixed", ptrs, pa.data_ptr(), pb.data_ptr(), half.data_ptr(), nx, ny, nz, pitch, it, 20, om,
                 gosa.data_ptr(), ctypes.byref(ci), sp.cuda_stream)
 
     lups = nx * ny * nz * it
@@ -404,20 +471,29 @@ def bench_himeno(torch, gb, W, dev, sp, hbm):
     ms_m = _time(torch, sp, mixed)
     out_m = (pa if ci.value == 0 else pb).clone()
     g_m = gosa.clone()
-    # one sweep of each kernel alone (average over 20 launches)
-    one = lambda: gb.call("appfis_gb_himeno", ptrs, pa.data_ptr(), pb.data_ptr(), nx, ny, nz, nx + 2, 20, om, gosa.data_ptr(),
-                          ctypes.byref(ci), sp.cuda_stream)
-    sweep_ms = _time(torch, sp, one, reps=1) / 20
-    gbs = nx * ny * nz * 56 / (sweep_ms * 1e-3) / 1e9
-    res["plain"] = {"glups": lups / (ms_p * 1e-3) / 1e9, "ms": ms_p, "bytes_per_lup": 56, "sweep_ms": sweep_ms,
-                    "achieved_gbs": gbs, "frac_of_hbm": gbs / hbm, "gosa_last": float(g_p[-1].item())}
+
+    def sweep_ms(ptr_list, a, b, pt, n=20):
+        one = lambda: gb.call("appfis_gb_himeno", ptr_list, a.data_ptr(), b.data_ptr(), nx, ny, nz, pt, n, om,
+                              gosa.data_ptr(), ctypes.byref(ci), sp.cuda_stream)
+        return _time(torch, sp, one, reps=1) / n
+
+    tma_ms = sweep_ms(ptrs, pa, pb, pitch)
+    dptrs = (ctypes.c_void_p * 12)(*[coef_d[k].data_ptr() for k in range(12)])
+    da, db = p0_d.clone(), p0_d.clone()
+    ring_ms = sweep_ms(dptrs, da, db, nx + 2)
+    del da, db
+    gbs = nx * ny * nz * 56 / (tma_ms * 1e-3) / 1e9
+    res["plain"] = {"glups": lups / (ms_p * 1e-3) / 1e9, "ms": ms_p, "bytes_per_lup": 56, "sweep_ms": tma_ms,
+                    "kernel": "himeno_tma<plain>", "achieved_gbs": gbs, "frac_of_hbm": gbs / hbm,
+                    "traffic": profiled_traffic("himeno_tma<plain>"),
+                    "ring_kernel_sweep_ms_dense_rows": ring_ms, "gosa_last": float(g_p[-1].item())}
     b_m = (19 * 30 + 62) / 20.0
     res["mixed_fp16_defect_correction"] = {
         "glups": lups / (ms_m * 1e-3) / 1e9, "ms": ms_m, "bytes_per_lup_avg": b_m, "period": 20,
         "speedup_vs_plain": ms_p / ms_m, "max_abs_diff_vs_plain_fp32": float((out_m - out_p).abs().max().item()),
         "gosa_last": float(g_m[-1].item()),
         "gosa_rel_diff_vs_plain": float(((g_m - g_p).abs() / g_p.abs().clamp_min(1e-300)).max().item())}
-    res["workload"] = "himeno 257x257x513 FP32, 400 iterations, per-sweep FP64 gosa"
+    res["workload"] = "himeno 257x257x513 FP32, 400 iterations, per-sweep FP64 gosa; rows padded to %d" % pitch
     return res
 
 
@@ -528,15 +604,16 @@ def profile_small(name, torch, gb, W, dev, sp):
     elif name == "himeno":
         c = W.HIMENO
         nx, ny, nz = c["nx"], c["ny"], c["nz"]
-        coef = torch.from_numpy(W.himeno_coef(nx, ny, nz)).to(dev)
-        p0 = torch.from_numpy(W.himeno_p(nx, ny, nz)).to(dev)
+        pitch = (nx + 2 + 7) // 8 * 8  # 16-byte rows: the TMA-staged kernels
+        coef = _pad_x(torch.from_numpy(W.himeno_coef(nx, ny, nz)).to(dev), pitch)
+        p0 = _pad_x(torch.from_numpy(W.himeno_p(nx, ny, nz)).to(dev), pitch)
         ptrs = (ctypes.c_void_p * 12)(*[coef[k].data_ptr() for k in range(12)])
         pa, pb = p0.clone(), p0.clone()
         half = torch.empty(13 * p0.numel(), dtype=torch.float16, device=dev)
         gosa = torch.zeros(8, dtype=torch.float64, device=dev)
-        gb.call("appfis_gb_himeno", ptrs, pa.data_ptr(), pb.data_ptr(), nx, ny, nz, nx + 2, 5, c["omega"], gosa.data_ptr(),
+        gb.call("appfis_gb_himeno", ptrs, pa.data_ptr(), pb.data_ptr(), nx, ny, nz, pitch, 5, c["omega"], gosa.data_ptr(),
                 ctypes.byref(ci), sp.cuda_stream)
-        gb.call("appfis_gb_himeno_mixed", ptrs, pa.data_ptr(), pb.data_ptr(), half.data_ptr(), nx, ny, nz, nx + 2, 5, 20,
+        gb.call("appfis_gb_himeno_mixed", ptrs, pa.data_ptr(), pb.data_ptr(), half.data_ptr(), nx, ny, nz, pitch, 5, 20,
                 c["omega"], gosa.data_ptr(), ctypes.byref(ci), sp.cuda_stream)
     elif name == "fdtd":
         c = W.FDTD
@@ -556,7 +633,8 @@ def profile_case(name, local):
     """Short fixed launch sequences for ncu captures.
     life:   16384^2 GameOfLife, 20 bit-packed generations (one life_bits_tb launch of 16 + 4
             life_bits_sweep) then 20 u8 sweeps (life_u8_swar)
-    himeno: 257x257x513, 5 plain sweeps (himeno_sweep), 5 mixed sweeps (himeno_inner, himeno_correct)
+    himeno: 257x257x513 (rows padded to 264), 5 plain sweeps (himeno_tma<0>), 5 mixed sweeps
+            (himeno_tma<1>, himeno_correct)
     fdtd:   512^3, 5 FP32 steps then 5 FP16 steps (star_r4_sweep)
     heat:   1024^2, 16 iterations (2 heat2d_blocked launches)
     flood:  4 domains of 512^2, 10 steps (one flood_persistent launch)"""
