@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "gb_common.cuh"
+#include "tma.cuh"
 
 namespace gb {
 
@@ -42,6 +43,9 @@ std::mutex g_mu;
 std::vector<std::vector<Buf>> g_dev;  // [device][slot]
 Buf g_pinned[2];
 std::vector<int> g_sms;
+std::vector<unsigned*> g_status;  // [device]
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
 }  // namespace
 
 int workspace(int slot, size_t bytes, void** out)
@@ -99,6 +103,64 @@ int sm_count()
     return g_sms[dev];
 }
 
+int status_word(unsigned** out)
+{
+    int dev = 0;
+    GB_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_mu);
+    if ((int)g_status.size() <= dev) g_status.resize(dev + 1, nullptr);
+    if (!g_status[dev]) {
+        unsigned* p = nullptr;
+        GB_TRY(cuda_status(cudaMalloc(&p, 256), "cudaMalloc(status word)"));
+        GB_TRY(cuda_status(cudaMemset(p, 0, 256), "cudaMemset(status word)"));
+        g_status[dev] = p;
+    }
+    *out = g_status[dev];
+    return APPFIS_GB_OK;
+}
+
+int check_status(const char* what)
+{
+    int dev = 0;
+    GB_CUDA(cudaGetDevice(&dev));
+    unsigned* p = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if ((int)g_status.size() > dev) p = g_status[dev];
+    }
+    if (!p) return APPFIS_GB_OK;
+    unsigned v = 0;
+    GB_CUDA(cudaMemcpy(&v, p, sizeof v, cudaMemcpyDeviceToHost));
+    if (v == 0) return APPFIS_GB_OK;
+    GB_CUDA(cudaMemset(p, 0, sizeof v));
+    return fail(APPFIS_GB_ETIMEOUT, "%s: a device-side wait gave up (status 0x%x: %s)", what, v,
+                (v & ST_SMEM_ALIGN) ? "shared-memory staging misaligned" : "bulk copy did not complete within 1 s");
+}
+
+int tensor_map_3d(CUtensorMap* map, CUtensorMapDataType type, size_t esize, const void* base, uint64_t dx, uint64_t dy,
+                  uint64_t dz, uint64_t pitch, uint64_t py, uint32_t bx, uint32_t by)
+{
+    std::call_once(g_encode_once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        cudaGetLastError();
+    });
+    if (!g_encode) return fail(APPFIS_GB_ECUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    if (!aligned16(base) || (pitch * esize) % 16 != 0)
+        return fail(APPFIS_GB_EINVAL, "tensor map: base or row stride not 16-byte aligned");
+    const cuuint64_t dims[3] = {dx, dy, dz};
+    const cuuint64_t strides[2] = {pitch * esize, pitch * py * esize};
+    const cuuint32_t box[3] = {bx, by, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = g_encode(map, type, 3, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(APPFIS_GB_ECUDA, "cuTensorMapEncodeTiled failed (CUresult %d)", (int)r);
+    return APPFIS_GB_OK;
+}
+
 }  // namespace gb
 
 extern "C" {
@@ -109,7 +171,8 @@ int appfis_gb_version(void) { return 10000; }
 
 int appfis_gb_stream_sync(void* stream)
 {
-    return gb::cuda_status(cudaStreamSynchronize(gb::as_stream(stream)), "cudaStreamSynchronize");
+    GB_CUDA(cudaStreamSynchronize(gb::as_stream(stream)));
+    return gb::check_status("appfis_gb_stream_sync");
 }
 
 }  // extern "C"

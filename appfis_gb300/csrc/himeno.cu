@@ -25,6 +25,7 @@
 #include <type_traits>
 
 #include "gb_common.cuh"
+#include "tma.cuh"
 
 namespace {
 
@@ -82,6 +83,26 @@ __device__ __forceinline__ void gosa_reduce(double v, double* __restrict__ parti
     }
 }
 
+// Per-thread sum of squares in two floats (hi + lo, ~48 significant bits): the square is split
+// exactly with an FMA and added with an exact two-sum, so a thread's few dozen terms stay within
+// ~1e-13 relative of the exact sum with FP32 instructions only (this part's FP64 rate is a small
+// fraction of its FP32 rate, and one FP64 multiply-add per point would cost more than the
+// point's memory traffic).  The block and grid sums that follow are in double.
+struct SqAcc {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add_sq(float x)
+    {
+        const float p = __fmul_rn(x, x);
+        const float e = __fmaf_rn(x, x, -p);  // p + e == x*x exactly
+        const float s = __fadd_rn(hi, p);
+        const float bb = __fsub_rn(s, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));  // hi + p == s + err
+        hi = s;
+        lo = __fadd_rn(lo, __fadd_rn(err, e));
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
 // 19-point s0 in the reference's order, on any readable field F (F(di,dj,dk) -> float)
 #define HIMENO_S0(F, A0, A1, A2, B0, B1, B2, C0, C1, C2, W1)                                               \
     fadd(fadd(fadd(fadd(fadd(fadd(fadd(fadd(fadd(fmul(A0, F(1, 0, 0)), fmul(A1, F(0, 1, 0))), fmul(A2, F(0, 0, 1))), \
@@ -118,8 +139,8 @@ __global__ void __launch_bounds__(BX* BY) himeno_correct(Coef12 cf, const float*
     const int j = 1 + blockIdx.y * BY + threadIdx.y;
     const int k0 = 1 + blockIdx.z * kz, k1 = min(k0 + kz, nz + 1);
     if (i > nx || j > ny) return;
-    const size_t plane = (size_t)px * py;
-    size_t c = ((size_t)k0 * py + j) * px + i;
+    const ptrdiff_t plane = (ptrdiff_t)px * py;
+    ptrdiff_t c = ((ptrdiff_t)k0 * py + j) * px + i;
     for (int k = k0; k < k1; k++) {
 #define QF(di, dj, dk)                                                                                      \
     (__ldg(P + c + (ptrdiff_t)(di) + (ptrdiff_t)(dj) * px + (ptrdiff_t)(dk) * (ptrdiff_t)plane) +          \
@@ -229,7 +250,7 @@ __global__ void __launch_bounds__(RX* RY) himeno_ring(Coef12 cf, H10 hf, const v
         }
     }
     __syncthreads();
-    double g = 0.0;
+    SqAcc g;
     for (int k = k0; k < k1; k++) {
         const size_t cc = ((size_t)k * py + j) * px + i;
         // prefetch the next plane's coefficients
@@ -258,7 +279,7 @@ __global__ void __launch_bounds__(RX* RY) himeno_ring(Coef12 cf, H10 hf, const v
                 const float pc = RF(0, 0, 0);
                 const float ss = fmul(fsub(fmul(s0v, co[3]), pc), co[10]);
                 reinterpret_cast<float*>(pout)[cc] = fadd(pc, fmul(omega, ss));
-                g += (double)ss * (double)ss;
+                g.add_sq(ss);
             } else {
                 // neighbour sum N e (no wrk1), then e' = e + w*bnd*(a3*N e - e) + D
                 float ne = co[0] * RF(1, 0, 0) + co[1] * RF(0, 1, 0) + co[2] * RF(0, 0, 1);
@@ -270,7 +291,7 @@ __global__ void __launch_bounds__(RX* RY) himeno_ring(Coef12 cf, H10 hf, const v
                 const float v = e0 + omega * co[9] * (co[10] * ne - e0) + co[11];
                 reinterpret_cast<__half*>(pout)[cc] = __float2half_rn(v);
                 const float ss = (v - e0) * inv_omega;
-                g += (double)ss * (double)ss;
+                g.add_sq(ss);
             }
 #undef RF
         }
@@ -284,10 +305,168 @@ __global__ void __launch_bounds__(RX* RY) himeno_ring(Coef12 cf, H10 hf, const v
         }
         __syncthreads();
     }
-    if (gosa) gosa_reduce(g, partials, ticket, gosa);
+    if (gosa) gosa_reduce(g.value(), partials, ticket, gosa);
+}
+
+// ---------------------------------------------------------------- TMA-staged 2.5-D forms
+// Same tile, z-march and arithmetic as himeno_ring, but every stream is moved by the tensor
+// memory accelerator: for plane k, one pipeline stage holds the twelve per-point tiles of plane
+// k (32 x 8 each) and the iterated field's plane k+1 (40 x 10 FP32 or 48 x 10 FP16, the halo
+// included, its x origin rounded down to a 16-byte boundary).  Thread 0 keeps S stages in
+// flight; the other threads only read shared memory.  The CTA's x tile starts on a 32-point
+// boundary of the padded row (thread tx owns padded x = 32*bx + tx, interior points only), so
+// every tile copy starts 16-byte aligned; this needs a pitch of a multiple of 4 (FP32) or 8
+// (FP16) elements and 16-byte aligned fields.
+struct TileMaps {
+    CUtensorMap m[13];  // 0..11: the per-point fields (see himeno_tma), 12: the iterated field
+};
+
+template <int MODE>
+struct TmaLayout {
+    typedef typename std::conditional<MODE == 0, float, __half>::type L;
+    static constexpr int XO = MODE == 0 ? 4 : 8;          // ring box x origin = tile x - XO
+    static constexpr int W = RX + 2 * XO;                 // ring box width (40 / 48)
+    static constexpr int RB = W * (RY + 2) * (int)sizeof(L);  // ring box bytes
+    static constexpr int PB = (RB + 127) / 128 * 128;     // ring slot bytes
+    static constexpr int CT = MODE == 0 ? 12 * 1024 : 10 * 512 + 1024 + 512;  // per-point tiles of one plane
+    __host__ __device__ static constexpr int tile_off(int n) { return MODE == 0 ? n * 1024 : (n < 10 ? n * 512 : (n == 10 ? 5120 : 6144)); }
+    static constexpr int smem(int S) { return S * CT + (S + 2) * PB + S * 8; }
+};
+
+template <int MODE, int S>
+__global__ void __launch_bounds__(RX* RY) himeno_tma(const __grid_constant__ TileMaps maps, void* __restrict__ pout, int nx, int ny,
+                                                      int nz, int pitch, int py, int kz, float omega, float inv_omega,
+                                                      double* __restrict__ partials, unsigned* __restrict__ ticket,
+                                                      double* __restrict__ gosa, unsigned* __restrict__ status)
+{
+    typedef TmaLayout<MODE> Lay;
+    typedef typename Lay::L L;
+    constexpr int P = S + 2;  // ring slots: planes k-1 .. k+S
+    extern __shared__ __align__(128) unsigned char tsm[];
+    unsigned char* stages = tsm;
+    unsigned char* slots = tsm + S * Lay::CT;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(tsm + S * Lay::CT + P * Lay::PB);
+
+    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * RX + tx;
+    const int x0 = blockIdx.x * RX, y0 = 1 + blockIdx.y * RY;
+    const int i = x0 + tx, j = y0 + ty;
+    const int k0 = 1 + blockIdx.z * kz, k1 = min(k0 + kz, nz + 1);
+    const bool act = i >= 1 && i <= nx && j <= ny;
+    if (gb::tma::smem_u32(tsm) & 127u) {  // uniform: the copies need 128-byte aligned destinations
+        if (t == 0) atomicOr(status, (unsigned)gb::ST_SMEM_ALIGN);
+        if (gosa) gosa_reduce(__longlong_as_double(0x7ff8000000000000ll), partials, ticket, gosa);
+        return;
+    }
+    if (t == 0) {
+#pragma unroll
+        for (int s = 0; s < S; s++) gb::tma::bar_init(&bar[s], 1);
+        gb::tma::fence_init();
+        for (int n = 0; n < 13; n++) gb::tma::prefetch_map(&maps.m[n]);
+    }
+    __syncthreads();
+
+    auto slot = [&](int pl) { return slots + ((pl - (k0 - 1)) % P) * Lay::PB; };
+    // thread 0: stage of plane k = the per-point tiles of plane k and the iterated field's plane k+1
+    // (the first stage also brings planes k0-1 and k0)
+    auto issue = [&](int k) {
+        const int s = (k - k0) % S;
+        unsigned char* st = stages + s * Lay::CT;
+        gb::tma::arrive_expect(&bar[s], Lay::CT + Lay::RB * (k == k0 ? 3 : 1));
+        if (k == k0) {
+            gb::tma::load_3d(slot(k0 - 1), &maps.m[12], x0 - Lay::XO, y0 - 1, k0 - 1, &bar[s]);
+            gb::tma::load_3d(slot(k0), &maps.m[12], x0 - Lay::XO, y0 - 1, k0, &bar[s]);
+        }
+#pragma unroll
+        for (int n = 0; n < 12; n++) gb::tma::load_3d(st + Lay::tile_off(n), &maps.m[n], x0, y0, k, &bar[s]);
+        gb::tma::load_3d(slot(k + 1), &maps.m[12], x0 - Lay::XO, y0 - 1, k + 1, &bar[s]);
+    };
+    if (t == 0)
+        for (int k = k0; k < min(k0 + S, k1); k++) issue(k);
+
+    SqAcc g;
+    bool bad = false;
+    int k = k0;
+    const int cq = ty * RX + tx;                        // this point in a per-point tile
+    const int q = (ty + 1) * Lay::W + tx + Lay::XO;     // this point in a ring slot
+    for (; k < k1; k++) {
+        const int s = (k - k0) % S;
+        if (!gb::tma::wait(&bar[s], (unsigned)((k - k0) / S) & 1u)) bad = true;
+        if (act && !bad) {
+            const unsigned char* st = stages + s * Lay::CT;
+            const L* sm = reinterpret_cast<const L*>(slot(k - 1));
+            const L* s0 = reinterpret_cast<const L*>(slot(k));
+            const L* sp = reinterpret_cast<const L*>(slot(k + 1));
+            const size_t cc = ((size_t)k * py + j) * pitch + i;
+            float co[12];
+            if (MODE == 0) {
+#pragma unroll
+                for (int n = 0; n < 12; n++) co[n] = reinterpret_cast<const float*>(st + Lay::tile_off(n))[cq];
+            } else {
+#pragma unroll
+                for (int n = 0; n < 10; n++) co[n] = __half2float(reinterpret_cast<const __half*>(st + Lay::tile_off(n))[cq]);
+                co[10] = reinterpret_cast<const float*>(st + Lay::tile_off(10))[cq];
+                co[11] = __half2float(reinterpret_cast<const __half*>(st + Lay::tile_off(11))[cq]);
+            }
+#define RF(di, dj, dk) ((float)(((dk) < 0 ? sm : ((dk) > 0 ? sp : s0))[q + (di) + (dj) * Lay::W]))
+            if (MODE == 0) {
+                const float s0v = HIMENO_S0(RF, co[0], co[1], co[2], co[4], co[5], co[6], co[7], co[8], co[9], co[11]);
+                const float pc = RF(0, 0, 0);
+                const float ss = fmul(fsub(fmul(s0v, co[3]), pc), co[10]);
+                reinterpret_cast<float*>(pout)[cc] = fadd(pc, fmul(omega, ss));
+                g.add_sq(ss);
+            } else {
+                float ne = co[0] * RF(1, 0, 0) + co[1] * RF(0, 1, 0) + co[2] * RF(0, 0, 1);
+                ne += co[3] * ((RF(1, 1, 0) - RF(1, -1, 0)) - (RF(-1, 1, 0) - RF(-1, -1, 0)));
+                ne += co[4] * ((RF(0, 1, 1) - RF(0, -1, 1)) - (RF(0, 1, -1) - RF(0, -1, -1)));
+                ne += co[5] * ((RF(1, 0, 1) - RF(-1, 0, 1)) - (RF(1, 0, -1) - RF(-1, 0, -1)));
+                ne += co[6] * RF(-1, 0, 0) + co[7] * RF(0, -1, 0) + co[8] * RF(0, 0, -1);
+                const float e0 = RF(0, 0, 0);
+                const float v = e0 + omega * co[9] * (co[10] * ne - e0) + co[11];
+                reinterpret_cast<__half*>(pout)[cc] = __float2half_rn(v);
+                g.add_sq((v - e0) * inv_omega);
+            }
+#undef RF
+        }
+        // everyone is done with stage s and with the slot of plane k-1: refill them with plane k+S
+        if (__syncthreads_or(bad)) break;
+        if (t == 0 && k + S < k1) issue(k + S);
+    }
+    if (k < k1) {  // a wait gave up: report, let the copies still in flight land, poison gosa
+        if (t == 0) {
+            atomicOr(status, (unsigned)gb::ST_TMA_TIMEOUT);
+            for (int kk = k; kk < min(k + S, k1); kk++) gb::tma::wait(&bar[(kk - k0) % S], (unsigned)((kk - k0) / S) & 1u);
+        }
+    }
+    if (gosa) gosa_reduce(k < k1 ? __longlong_as_double(0x7ff8000000000000ll) : g.value(), partials, ticket, gosa);
+}
+
+// z planes per CTA: about HKZ, balanced so that no chunk is much shorter than the others
+inline int balanced_kz(int nz, int target)
+{
+    const int chunks = (nz + target - 1) / target;
+    return (nz + chunks - 1) / chunks;
 }
 
 constexpr int HBX = 32, HBY = 4, HKZ = 32;
+constexpr int TMA_S_PLAIN = 3, TMA_S_MIXED = 4;
+
+// Tensor maps of the plain form: the 12 FP32 coefficient fields and the iterated p buffer.
+int plain_maps(const float* const* coef, const float* pin, int nx, int ny, int nz, int pitch, TileMaps* m)
+{
+    const int py = ny + 2;
+    for (int n = 0; n < 12; n++)
+        GB_TRY(gb::tensor_map_3d(&m->m[n], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, coef[n], nx + 2, py, nz + 2, pitch, py, RX, RY));
+    return gb::tensor_map_3d(&m->m[12], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pin, nx + 2, py, nz + 2, pitch, py,
+                             TmaLayout<0>::W, RY + 2);
+}
+
+bool plain_tma_ok(const float* const* coef, const float* p, const float* wrk2, int pitch)
+{
+    if (pitch % 4 != 0 || !gb::aligned16(p) || !gb::aligned16(wrk2)) return false;
+    for (int n = 0; n < 12; n++)
+        if (!gb::aligned16(coef[n])) return false;
+    return true;
+}
 
 int check_dims(int nx, int ny, int nz, int pitch)
 {
@@ -325,10 +504,33 @@ int appfis_gb_himeno(const float* const* coef, float* p, float* wrk2, int nx, in
     dim3 blk(RX, RY), grd(gb::ceil_div(nx, RX), gb::ceil_div(ny, RY), gb::ceil_div(nz, HKZ));
     double* partials = nullptr;
     unsigned* ticket = nullptr;
-    if (dev_gosa) GB_TRY(gosa_scratch(grd, &partials, &ticket, st));
     float* buf[2] = {p, wrk2};
-    H10 none = {};
     int ci = 0;
+    if (plain_tma_ok(coef, p, wrk2, pitch)) {
+        // TMA-staged form: tile x origins on 32-point boundaries of the padded row
+        TileMaps maps[2];
+        GB_TRY(plain_maps(coef, p, nx, ny, nz, pitch, &maps[0]));
+        maps[1] = maps[0];
+        GB_TRY(gb::tensor_map_3d(&maps[1].m[12], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, wrk2, nx + 2, ny + 2, nz + 2, pitch,
+                                 ny + 2, TmaLayout<0>::W, RY + 2));
+        unsigned* status;
+        GB_TRY(gb::status_word(&status));
+        const int kz = balanced_kz(nz, HKZ);
+        dim3 tgrd(nx / RX + 1, gb::ceil_div(ny, RY), gb::ceil_div(nz, kz));
+        if (dev_gosa) GB_TRY(gosa_scratch(tgrd, &partials, &ticket, st));
+        constexpr int smem = TmaLayout<0>::smem(TMA_S_PLAIN);
+        GB_CUDA(cudaFuncSetAttribute(himeno_tma<0, TMA_S_PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        for (int it = 0; it < iters; it++) {
+            himeno_tma<0, TMA_S_PLAIN><<<tgrd, blk, smem, st>>>(maps[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2, kz, omega, 0.0f,
+                                                               partials, ticket, dev_gosa ? dev_gosa + it : nullptr, status);
+            ci = 1 - ci;
+        }
+        GB_TRY(gb::launched("himeno_tma<plain>"));
+        if (cur_index) *cur_index = ci;
+        return APPFIS_GB_OK;
+    }
+    if (dev_gosa) GB_TRY(gosa_scratch(grd, &partials, &ticket, st));
+    H10 none = {};
     for (int it = 0; it < iters; it++) {
         himeno_ring<0><<<grd, blk, 0, st>>>(cf, none, buf[ci], buf[1 - ci], nullptr, nx, ny, nz, pitch, ny + 2, HKZ, omega, 0.0f,
                                             partials, ticket, dev_gosa ? dev_gosa + it : nullptr);
@@ -364,9 +566,29 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     himeno_half_coef<<<dim3(gb::ceil_div(nx, 128), ny, nz), 128, 0, st>>>(cf, Hc, field, nx, ny, nz, pitch, ny + 2);
     dim3 blk(HBX, HBY), grd(gb::ceil_div(nx, HBX), gb::ceil_div(ny, HBY), gb::ceil_div(nz, HKZ));
     dim3 rblk(RX, RY), rgrd(gb::ceil_div(nx, RX), gb::ceil_div(ny, RY), gb::ceil_div(nz, HKZ));
+    // TMA-staged inner sweeps when the FP16 rows are 16-byte aligned (pitch a multiple of 8)
+    const bool use_tma = pitch % 8 == 0 && gb::aligned16(hw) && gb::aligned16(coef[3]);
+    const int tkz = balanced_kz(nz, HKZ);
+    dim3 tgrd(nx / RX + 1, gb::ceil_div(ny, RY), gb::ceil_div(nz, tkz));
+    TileMaps tmaps[2];
+    unsigned* status = nullptr;
+    constexpr int tsmem = TmaLayout<1>::smem(TMA_S_MIXED);
+    if (use_tma) {
+        const int py = ny + 2;
+        for (int n = 0; n < 10; n++)
+            GB_TRY(gb::tensor_map_3d(&tmaps[0].m[n], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, hf.c[n], nx + 2, py, nz + 2, pitch, py, RX, RY));
+        GB_TRY(gb::tensor_map_3d(&tmaps[0].m[10], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, coef[3], nx + 2, py, nz + 2, pitch, py, RX, RY));
+        GB_TRY(gb::tensor_map_3d(&tmaps[0].m[11], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, Dd, nx + 2, py, nz + 2, pitch, py, RX, RY));
+        tmaps[1] = tmaps[0];
+        for (int b = 0; b < 2; b++)
+            GB_TRY(gb::tensor_map_3d(&tmaps[b].m[12], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, E[b], nx + 2, py, nz + 2, pitch, py,
+                                     TmaLayout<1>::W, RY + 2));
+        GB_TRY(gb::status_word(&status));
+        GB_CUDA(cudaFuncSetAttribute(himeno_tma<1, TMA_S_MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem));
+    }
     double* rpartials = nullptr;
     unsigned* rticket = nullptr;
-    if (dev_gosa) GB_TRY(gosa_scratch(rgrd, &rpartials, &rticket, st));
+    if (dev_gosa) GB_TRY(gosa_scratch(use_tma ? tgrd : rgrd, &rpartials, &rticket, st));
     float* P[2] = {p, p_work};
     int pc = 0, ec = 0;
     // D from the initial P (e = 0), e restarted at 0
@@ -375,8 +597,13 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     ec = 1 - ec;
     const float inv_omega = 1.0f / omega;
     for (int it = 0; it < iters; it++) {
-        himeno_ring<1><<<rgrd, rblk, 0, st>>>(cf, hf, E[ec], E[1 - ec], Dd, nx, ny, nz, pitch, ny + 2, HKZ, omega, inv_omega,
-                                              rpartials, rticket, dev_gosa ? dev_gosa + it : nullptr);
+        if (use_tma)
+            himeno_tma<1, TMA_S_MIXED><<<tgrd, rblk, tsmem, st>>>(tmaps[ec], E[1 - ec], nx, ny, nz, pitch, ny + 2, tkz, omega,
+                                                                 inv_omega, rpartials, rticket,
+                                                                 dev_gosa ? dev_gosa + it : nullptr, status);
+        else
+            himeno_ring<1><<<rgrd, rblk, 0, st>>>(cf, hf, E[ec], E[1 - ec], Dd, nx, ny, nz, pitch, ny + 2, HKZ, omega, inv_omega,
+                                                  rpartials, rticket, dev_gosa ? dev_gosa + it : nullptr);
         ec = 1 - ec;
         if ((it + 1) % period == 0 || it + 1 == iters) {
             himeno_correct<HBX, HBY><<<grd, blk, 0, st>>>(cf, P[pc], E[ec], P[1 - pc], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2,

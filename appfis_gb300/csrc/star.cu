@@ -20,6 +20,7 @@
 #include <cuda_fp16.h>
 
 #include "gb_common.cuh"
+#include "tma.cuh"
 
 namespace {
 
@@ -296,6 +297,163 @@ __global__ void __launch_bounds__(256) star_r4_vec(const T* __restrict__ in, T* 
     }
 }
 
+// ---------------------------------------------------------------- TMA-staged form
+// A 64 x 16 (x, y) tile per CTA; each thread owns 4 consecutive x points of RYT consecutive
+// rows, and every plane is moved by the tensor memory accelerator: plane pl arrives as one
+// 72 x 24 box (the x/y halo included; the box x origin is the tile's first ghost column, a
+// 64-point boundary of the padded row, so every copy starts 16-byte aligned) in slot
+// (pl - k0 + 4) % TNS of a shared ring, signalled on that slot's mbarrier.  Thread 0 keeps
+// TNS - 5 planes in flight beyond the newest one in use.  Each thread pushes its centre values
+// of plane k+4 into its z queue (registers); the x/y windows of plane k come from the ring, except
+// the thread's own rows, which are the queue's centre entries.  With RYT = 2 a thread reads 14
+// 16-byte shared vectors per 8 points (2 queue pushes, 2 x 2 x-windows, 8 y-window rows) instead
+// of 12 per 4.  Global traffic: each plane read once per CTA (plus the 8-plane z-chunk overlap),
+// each result written once.
+constexpr int TNS = 8;                   // ring slots: planes k..k+4 resident, 3 more in flight
+constexpr int TSW = VTX + 2 * R, TSH = VTY + 2 * R;
+constexpr int TRY = 2;                   // rows per thread
+
+template <class T>
+struct TmaStar {
+    static constexpr int BOX = TSW * TSH * (int)sizeof(T);  // bytes per plane box
+    static constexpr int SLOT = (BOX + 127) / 128 * 128;
+    static constexpr int smem() { return TNS * SLOT + TNS * 8; }
+};
+
+template <class T> __device__ __forceinline__ float4 lds4(const T* p);
+template <> __device__ __forceinline__ float4 lds4<float>(const float* p) { return *reinterpret_cast<const float4*>(p); }
+template <> __device__ __forceinline__ float4 lds4<__half>(const __half* p)
+{
+    const uint2 u = *reinterpret_cast<const uint2*>(p);
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+}
+
+template <class T, int MODE, int RYT>
+__global__ void __launch_bounds__(16 * (VTY / RYT)) star_r4_tma(const __grid_constant__ CUtensorMap map, T* __restrict__ out,
+                                                               int nx, int ny, int nz, int px, int py, int kz, float coeff,
+                                                               StarW wt, unsigned* __restrict__ status)
+{
+    typedef TmaStar<T> Lay;
+    extern __shared__ __align__(128) unsigned char tsm[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(tsm + TNS * Lay::SLOT);
+    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * 16 + tx;
+    const int bx0 = blockIdx.x * VTX, by0 = blockIdx.y * VTY;  // box origin (padded coordinates)
+    const int x = R + bx0 + VX * tx, y = R + by0 + RYT * ty;    // this thread's first point
+    const int k0 = R + blockIdx.z * kz, k1 = min(k0 + kz, nz + R);
+    const int plast = k1 + R - 1;                               // last plane the chunk reads
+    const size_t plane = (size_t)px * py;
+    if (gb::tma::smem_u32(tsm) & 127u) {
+        if (t == 0) atomicOr(status, (unsigned)gb::ST_SMEM_ALIGN);
+        return;
+    }
+    if (t == 0) {
+        for (int n = 0; n < TNS; n++) gb::tma::bar_init(&bar[n], 1);
+        gb::tma::fence_init();
+        gb::tma::prefetch_map(&map);
+    }
+    __syncthreads();
+    const int pbase = k0 - R;  // plane of slot 0, phase 0
+    auto slot = [&](int pl) { return reinterpret_cast<const T*>(tsm + ((pl - pbase) % TNS) * Lay::SLOT); };
+    int last_issued = pbase - 1;  // thread 0 only
+    auto issue = [&](int pl) {
+        last_issued = pl;
+        const int n = (pl - pbase) % TNS;
+        gb::tma::arrive_expect(&bar[n], Lay::BOX);
+        gb::tma::load_3d(tsm + n * Lay::SLOT, &map, bx0, by0, pl, &bar[n]);
+    };
+    auto ready = [&](int pl) { return gb::tma::wait(&bar[(pl - pbase) % TNS], (unsigned)((pl - pbase) / TNS) & 1u); };
+    if (t == 0)
+        for (int pl = pbase; pl < pbase + TNS && pl <= plast; pl++) issue(pl);
+
+    const int own = (RYT * ty + R) * TSW + R + VX * tx;  // this thread's first row, 4 points, in a slot
+    bool bad = false;
+    float4 q[RYT][9];
+#pragma unroll
+    for (int m = 0; m < 8; m++) {  // planes k0-4 .. k0+3
+        if (!bad && !ready(pbase + m)) bad = true;
+#pragma unroll
+        for (int r = 0; r < RYT; r++) q[r][m] = lds4<T>(slot(pbase + m) + own + r * TSW);
+    }
+    // planes k0-4 .. k0-1 only fed the queue: their slots take planes pbase+8 .. pbase+11
+    bad = __syncthreads_or(bad);
+    if (t == 0 && !bad)
+        for (int pl = pbase + TNS; pl < pbase + TNS + R && pl <= plast; pl++) issue(pl);
+
+    for (int kb = k0; kb < k1 && !bad; kb += 9) {
+#pragma unroll
+        for (int P = 0; P < 9; P++) {
+            const int k = kb + P;
+            if (k < k1 && !bad) {
+                if (!ready(k + R)) bad = true;
+#pragma unroll
+                for (int r = 0; r < RYT; r++) q[r][(P + 8) % 9] = lds4<T>(slot(k + R) + own + r * TSW);
+                const T* rowp = slot(k) + own;
+                // y-window rows m = -4..-1 and RYT..RYT+3 relative to the first row
+                float4 wv[8];
+#pragma unroll
+                for (int a = 1; a <= R; a++) {
+                    wv[a - 1] = lds4<T>(rowp - a * TSW);
+                    wv[R + a - 1] = lds4<T>(rowp + (RYT - 1 + a) * TSW);
+                }
+#pragma unroll
+                for (int r = 0; r < RYT; r++) {
+                    const float4 xl = lds4<T>(rowp + r * TSW - 4), xc = q[r][(P + 4) % 9], xr = lds4<T>(rowp + r * TSW + 4);
+                    const float xw[12] = {xl.x, xl.y, xl.z, xl.w, xc.x, xc.y, xc.z, xc.w, xr.x, xr.y, xr.z, xr.w};
+                    float4 ym[R], yp[R];
+#pragma unroll
+                    for (int a = 1; a <= R; a++) {
+                        const int mm = r - a, mp = r + a;  // rows relative to the first row
+                        ym[a - 1] = mm >= 0 ? q[mm < RYT ? mm : 0][(P + 4) % 9] : wv[-mm - 1];
+                        yp[a - 1] = mp < RYT ? q[mp][(P + 4) % 9] : wv[R + mp - RYT];
+                    }
+                    float res[4];
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const float cen = xw[4 + c];
+                        float v;
+                        if (MODE == 0) {
+                            v = cen;
+#pragma unroll
+                            for (int a = 1; a <= R; a++) {
+                                const float sx = __fadd_rn(xw[4 + c - a], xw[4 + c + a]);
+                                const float sy = __fadd_rn(f4(ym[a - 1], c), f4(yp[a - 1], c));
+                                const float sz = __fadd_rn(f4(q[r][(P + 4 - a) % 9], c), f4(q[r][(P + 4 + a) % 9], c));
+                                v = __fadd_rn(v, __fadd_rn(__fadd_rn(sx, sy), sz));
+                            }
+                            v = __fmul_rn(v, coeff);
+                        } else {
+                            v = wt.w[0] * cen;
+#pragma unroll
+                            for (int a = 1; a <= R; a++)
+                                v += wt.w[a] * (((xw[4 + c - a] + xw[4 + c + a]) + (f4(ym[a - 1], c) + f4(yp[a - 1], c))) +
+                                                (f4(q[r][(P + 4 - a) % 9], c) + f4(q[r][(P + 4 + a) % 9], c)));
+                        }
+                        res[c] = v;
+                    }
+                    const int yr = y + r;
+                    if (!bad && x < nx + R && yr < ny + R) {
+                        T* o = out + (size_t)k * plane + (size_t)yr * px + x;
+                        if (x + VX <= nx + R) {
+                            Vec4<T>::st(o, make_float4(res[0], res[1], res[2], res[3]));
+                        } else {  // ragged last vector of a row: only the interior lanes
+                            for (int c = 0; c < VX && x + c < nx + R; c++) st<T>(o + c, res[c]);
+                        }
+                    }
+                }
+                // plane k's slot is free once every thread is past this barrier: it takes plane k+TNS
+                bad = __syncthreads_or(bad);
+                if (t == 0 && !bad && k + TNS <= plast) issue(k + TNS);
+            }
+        }
+    }
+    if (bad && t == 0) {  // a wait gave up: report and let the copies still in flight land
+        atomicOr(status, (unsigned)gb::ST_TMA_TIMEOUT);
+        for (int pl = max(pbase, last_issued - TNS + 1); pl <= last_issued; pl++) ready(pl);  // latest phase of each slot
+    }
+}
+
 template <class T, int MODE, int RY>
 void launch_star(const T* in, T* out, int nx, int ny, int nz, int px, int kz, float coeff, StarW w, cudaStream_t st)
 {
@@ -312,10 +470,34 @@ int run_star(T* a, T* b, int nx, int ny, int nz, int pitch, int iters, int mode,
     if (w5)
         for (int n = 0; n < 5; n++) w.w[n] = w5[n];
     T* buf[2] = {a, b};
-    const int align = sizeof(T) == 4 ? 4 : 4;  // elements per vector: rows and base must allow 4-wide access
-    const bool vec = ry == 0 && pitch % align == 0 && ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) %
-                                                          (sizeof(T) * 4)) == 0;
+    // TMA-staged tile when the rows are 16-byte aligned; else the register-staged vector tile when
+    // 4-element vectors are aligned; else the scalar tile
+    const bool tma = ry == 0 && (pitch * sizeof(T)) % 16 == 0 && gb::aligned16(a) && gb::aligned16(b);
+    const bool vec = ry == 0 && pitch % 4 == 0 && ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) %
+                                                    (sizeof(T) * 4)) == 0;
     int ci = 0;
+    if (tma) {
+        const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+        CUtensorMap maps[2];
+        for (int n = 0; n < 2; n++)
+            GB_TRY(gb::tensor_map_3d(&maps[n], dt, sizeof(T), buf[n], nx + 2 * R, ny + 2 * R, nz + 2 * R, pitch, ny + 2 * R, TSW,
+                                     TSH));
+        unsigned* status;
+        GB_TRY(gb::status_word(&status));
+        constexpr int smem = TmaStar<T>::smem();
+        auto kern = mode == 0 ? star_r4_tma<T, 0, TRY> : star_r4_tma<T, 1, TRY>;
+        GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        const int tkz = kz > 0 ? kz : 64;
+        dim3 blk(16, VTY / TRY), grd(gb::ceil_div(nx, VTX), gb::ceil_div(ny, VTY), gb::ceil_div(nz, tkz));
+        for (int it = 0; it < iters; it++) {
+            kern<<<grd, blk, smem, st>>>(maps[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2 * R, tkz, coeff, w, status);
+            ci = 1 - ci;
+        }
+        GB_TRY(gb::launched("star_r4_tma"));
+        if (cur_index) *cur_index = ci;
+        return APPFIS_GB_OK;
+    }
+    if (kz <= 0) kz = 32;
     for (int it = 0; it < iters; it++) {
         if (vec) {
             dim3 blk(16, 16), grd(gb::ceil_div(nx, VTX), gb::ceil_div(ny, VTY), gb::ceil_div(nz, kz));
@@ -349,7 +531,7 @@ int appfis_gb_star_r4(void* a, void* b, int dtype, int nx, int ny, int nz, int p
     if (iters < 0) return gb::fail(APPFIS_GB_EINVAL, "star_r4: negative iteration count");
     const int ry = tile_rows < 0 ? 0 : tile_rows;  // 0: vectorised tile when the rows are 16-byte aligned
     if (ry != 0 && ry != 2 && ry != 4) return gb::fail(APPFIS_GB_EINVAL, "star_r4: tile_rows must be 0, 2 or 4");
-    const int kz = zchunk <= 0 ? 32 : zchunk;
+    const int kz = zchunk <= 0 ? 0 : zchunk;  // 0: the kernel's default (64 planes TMA-staged, 32 otherwise)
     cudaStream_t st = gb::as_stream(stream);
     if (dtype == APPFIS_GB_F32)
         return run_star<float>((float*)a, (float*)b, nx, ny, nz, pitch, iters, mode, coeff, weights, ry, kz, cur_index, st);

@@ -177,6 +177,64 @@ def cpu_gol_sample(cells, gens):
     return nx * ny * gens / (time.perf_counter() - t) / 1e9, cores, "port"
 
 
+def cpu_app_samples():
+    """The reference's own OpenMP path (oracle/_ref harnesses, every host core) on a bounded
+    sample of each other workload: GLUP/s of the sweep loop only (the harness's timer)."""
+    from oracle import build_ref
+    from oracle import oracle as O
+    from appfis_gb300 import workloads as W
+
+    cores = os.cpu_count() or 1
+    out = {}
+
+    def one(name, fn):
+        if build_ref.exe_path(name) is None:
+            out[name] = {"unavailable": "reference harness not built"}
+            return
+        try:
+            lups, secs, sample = fn()
+            out[name] = {"glups": lups / secs / 1e9, "seconds": secs, "cores": cores, "kind": "reference",
+                         "sample": sample}
+        except Exception as e:  # report, do not hide
+            out[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+
+    def heat():
+        nx = ny = 1024
+        it = 400
+        f = W.heat2d_padded(nx, ny, 1.0, 42)
+        res, _ = O.run_ref("heat2d", [nx, ny, it, cores, 0.2, 1.0, "{in0}", "{out0}"],
+                           [np.ascontiguousarray(f[1:-1, 1:-1])], [(np.float32, 0)])
+        return nx * ny * it, res["seconds"], "1024x1024 FP32, %d of the 1000 iterations" % it
+
+    def himeno():
+        nx, ny, nz, it = 257, 257, 129, 10
+        coef = W.himeno_coef(nx, ny, nz)
+        p = W.himeno_p(nx, ny, nz)
+        res, _ = O.run_ref("himeno", [nx, ny, nz, it, cores, 0.8, "{in0}", "{in1}", "{out0}", "{out1}"],
+                           [coef, np.ascontiguousarray(p[1:-1, 1:-1, 1:-1])], [(np.float32, 0), (np.float64, 0)])
+        return nx * ny * nz * it, res["seconds"], "257x257x129 (a quarter of the z extent), %d sweeps" % it
+
+    def fdtd():
+        n, it = 512, 2
+        f = np.ascontiguousarray(W.fdtd_padded(n, n, n, 42)[4:-4, 4:-4, 4:-4])
+        res, _ = O.run_ref("fdtd", [n, n, n, it, cores, 0.1, "{in0}", "{out0}"], [f], [(np.float32, 0)])
+        return n ** 3 * it, res["seconds"], "512^3 FP32, %d steps of the reference form (same 25-point reads)" % it
+
+    def triton():
+        ny = nx = 1024
+        steps = 200
+        dem, h = W.triton_domain(ny, nx, 4242)
+        args = [nx, ny, cores, 10.0, 0.5, 1e-3, 0.035, 600.0, 600.0, 1.0, steps, "{in0}", "{in1}", "{out0}", "{out1}"]
+        res, _ = O.run_ref("triton", args, [dem, h], [(np.float64, 0), (np.float64, 0)])
+        return nx * ny * int(res["steps"]), res["seconds"], "one 1024x1024 domain, FP64, %d steps" % int(res["steps"])
+
+    one("heat2d", heat)
+    one("himeno", himeno)
+    one("fdtd", fdtd)
+    one("triton", triton)
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -360,6 +418,8 @@ def run_ours(args, rank, world, local):
                        ("himeno", lambda: bench_himeno(torch, gb, W2, dev, stream, hbm_peak)),
                        ("fdtd3d", lambda: bench_fdtd(torch, gb, W2, dev, stream, hbm_peak)),
                        ("flood", lambda: bench_flood(torch, gb, W2, dev, stream))):
+            if nm not in args.apps.split(","):
+                continue
             try:
                 per[nm] = fn()
             except Exception as e:  # report, do not hide: the line still carries the headline
@@ -369,6 +429,8 @@ def run_ours(args, rank, world, local):
         v, cores, kind = cpu_gol_sample(cells, args.ref_gens)
         line["cpu_baseline"] = {"value": v, "unit": "GLUP/s", "cores": cores, "kind": kind,
                                 "sample": "16384x16384 grid, %d generations" % args.ref_gens}
+        if not args.no_apps:
+            line["cpu_baseline"]["per_app"] = cpu_app_samples()
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -526,9 +588,11 @@ def bench_fdtd(torch, gb, W, dev, sp, hbm):
     g16 = nx * ny * nz * 4 / (s16 * 1e-3) / 1e9
     res["workload"] = "fdtd3d radius-4 star 512^3, 200 steps of u <- u + 0.1*L8(u), zero halo of 4"
     res["plain_fp32"] = {"glups": lups / (ms32 * 1e-3) / 1e9, "ms": ms32, "bytes_per_lup": 8, "sweep_ms": s32,
-                         "achieved_gbs": g32, "frac_of_hbm": g32 / hbm}
+                         "kernel": "star_r4_tma<float>", "achieved_gbs": g32, "frac_of_hbm": g32 / hbm,
+                         "traffic": profiled_traffic("star_r4_tma<float>")}
     res["fp16_storage"] = {"glups": lups / (ms16 * 1e-3) / 1e9, "ms": ms16, "bytes_per_lup": 4, "sweep_ms": s16,
-                           "achieved_gbs": g16, "frac_of_hbm": g16 / hbm, "speedup_vs_plain": ms32 / ms16,
+                           "kernel": "star_r4_tma<half>", "achieved_gbs": g16, "frac_of_hbm": g16 / hbm,
+                           "traffic": profiled_traffic("star_r4_tma<half>"), "speedup_vs_plain": ms32 / ms16,
                            "max_abs_diff_vs_fp32": float((o16 - o32).abs().max().item())}
     return res
 
@@ -635,7 +699,7 @@ def profile_case(name, local):
             life_bits_sweep) then 20 u8 sweeps (life_u8_swar)
     himeno: 257x257x513 (rows padded to 264), 5 plain sweeps (himeno_tma<0>), 5 mixed sweeps
             (himeno_tma<1>, himeno_correct)
-    fdtd:   512^3, 5 FP32 steps then 5 FP16 steps (star_r4_sweep)
+    fdtd:   512^3, 5 FP32 steps then 5 FP16 steps (star_r4_tma)
     heat:   1024^2, 16 iterations (2 heat2d_blocked launches)
     flood:  4 domains of 512^2, 10 steps (one flood_persistent launch)"""
     import torch
@@ -679,6 +743,7 @@ def main():
     ap.add_argument("--ref-gens", type=int, default=8, help="generations per CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-apps", action="store_true", help="skip the per-workload measurements")
+    ap.add_argument("--apps", default="heat2d,himeno,fdtd3d,flood", help="comma-separated per-workload measurements")
     ap.add_argument("--profile-case", choices=["life", "himeno", "fdtd", "heat", "flood"], default=None,
                     help="launch a short fixed sequence of the named workload's kernels (for ncu), no timing")
     args = ap.parse_args()

@@ -60,7 +60,9 @@ extern "C" {
 APPFIS_GB_API const char* appfis_gb_last_error(void);
 APPFIS_GB_API int appfis_gb_version(void);
 /* Blocks until all work on `stream` is done (replaces the reference's cudaStreamSynchronize
- * calls on its one stream, Appfis/Topology.hpp:151). */
+ * calls on its one stream, Appfis/Topology.hpp:151).  Then reads and clears the device status
+ * word that kernels with bounded device-side waits set when a wait gives up (the results of
+ * that launch are then invalid): returns APPFIS_GB_ETIMEOUT if it was set. */
 APPFIS_GB_API int appfis_gb_stream_sync(void* stream);
 
 /* ----------------------------------------------------------------------------- reductions */

@@ -62,6 +62,75 @@ def flatten(path, search, seen_once, out_lines):
         out_lines.append(line)
 
 
+# ------------------------------------------------------------------ the reference's applications
+# The five sample applications, unchanged, as test inputs for the drop-in headers: each
+# <app>/src/main.cpp is flattened twice into oracle/_ref/apps/ (git-ignored, never committed):
+#   <app>.ref.cpp   — with the reference's own Appfis headers and the MPI stand-in inlined (built
+#                     here with g++ and APPFIS_CPU: the reference's CPU path);
+#   <app>.gb.cpp    — with the application's own files inlined and every Appfis include replaced
+#                     by the drop-in's "Appfis.hpp" (built with nvcc by tests/dropin/build_apps.py).
+APPS = ["HeatDiffusion", "GameOfLife", "Himeno", "FDTD3d", "Triton"]
+APPS_DIR = os.path.join(OUT, "apps")
+
+
+def _flatten_app(path, search, seen, out_lines, appfis_dir, dropin):
+    if path in seen:
+        return
+    seen.add(path)
+    with open(path, "r", encoding="utf-8", errors="replace") as f:
+        lines = f.read().splitlines()
+    for line in lines:
+        m = INC_RE.match(line)
+        if m:
+            target = _resolve(m.group(1), os.path.dirname(path), search)
+            if target is not None:
+                if dropin and os.path.dirname(target) == appfis_dir:
+                    if "<appfis>" not in seen:
+                        seen.add("<appfis>")
+                        out_lines.append('#include "Appfis.hpp"')
+                    continue
+                _flatten_app(target, search, seen, out_lines, appfis_dir, dropin)
+                continue
+        if line.strip() == "#pragma once":
+            continue
+        out_lines.append(line)
+
+
+def app_source(app, variant):
+    return os.path.join(APPS_DIR, "%s.%s.cpp" % (app, variant))
+
+
+def make_app_flats():
+    """Writes the flattened application sources (needs the reference tree)."""
+    os.makedirs(APPS_DIR, exist_ok=True)
+    appfis_dir = os.path.normpath(os.path.join(REF_ROOT, "Appfis"))
+    for app in APPS:
+        main = os.path.join(REF_ROOT, app, "src", "main.cpp")
+        for variant, dropin in (("ref", False), ("gb", True)):
+            lines = []
+            search = [os.path.join(HERE, "mpi_stub")] if not dropin else []
+            _flatten_app(main, search, set(), lines, appfis_dir, dropin)
+            text = "\n".join(lines) + "\n"
+            path = app_source(app, variant)
+            if not (os.path.exists(path) and open(path).read() == text):
+                with open(path, "w") as f:
+                    f.write(text)
+
+
+def app_ref_exe(app):
+    """The reference CPU build of an application (built on first use), or None."""
+    src = app_source(app, "ref")
+    if not os.path.exists(src):
+        return None
+    exe = os.path.join(APPS_DIR, "%s.ref" % app)
+    if not (_runs_here(exe) and os.path.getmtime(exe) >= os.path.getmtime(src)):
+        cmd = ["g++", "-O2", "-fopenmp", "-ffp-contract=off", "-std=c++11", "-DAPPFIS_CPU=1", "-w", src, "-o", exe]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("building %s failed:\n%s" % (exe, r.stderr[-4000:]))
+    return exe
+
+
 def flat_path(name):
     return os.path.join(OUT, "ref_%s.flat.cpp" % name)
 
@@ -111,6 +180,8 @@ def build(jobs=8, quiet=True):
     """Build every harness that can be built here; return the list of executables."""
     os.makedirs(OUT, exist_ok=True)
     have_ref = os.path.isdir(os.path.join(REF_ROOT, "Appfis"))
+    if have_ref:
+        make_app_flats()
     names = []
     for name in HARNESSES:
         if have_ref:

@@ -150,7 +150,8 @@ def ref_available(name):
 def run_ref(name, args, inputs, outputs):
     """Run oracle/_ref/ref_<name> with raw-file inputs.  inputs: list of np arrays written to
     temp files (paths substituted for '{in0}', '{in1}', ...); outputs: list of (dtype, count)
-    read back from '{out0}', ....  Returns (json_dict, [arrays])."""
+    read back from '{out0}', ... (count None: the whole file, 0: not read).  Returns
+    (json_dict, [arrays])."""
     exe = build_ref.exe_path(name)
     if exe is None:
         raise RuntimeError("reference harness %s is not built on this machine" % name)
@@ -170,6 +171,9 @@ def run_ref(name, args, inputs, outputs):
         res = json.loads(line)
         outs = []
         for k, (dt, cnt) in enumerate(outputs):
+            if cnt == 0:  # not wanted
+                outs.append(None)
+                continue
             a = np.fromfile(subs["out%d" % k], dtype=dt)
             if cnt is not None:
                 a = a[:cnt]

@@ -87,3 +87,65 @@ def test_mixed_defect_correction_error(gb, torch_cuda):
     assert err_mixed < 2.5e-4, err_mixed
     np.testing.assert_allclose(gm, g64, rtol=1e-2)
     np.testing.assert_allclose(gp, g64, rtol=1e-4)
+
+
+def device_run(gb, torch, coef, p, iters, pitch, form=0, period=20, omega=0.8):
+    """Runs the device entry point on fields whose rows are padded to `pitch` elements."""
+    nz, ny, nx = p.shape[0] - 2, p.shape[1] - 2, p.shape[2] - 2
+    hp = np.zeros((nz + 2, ny + 2, pitch), dtype=np.float32)
+    hp[:, :, : nx + 2] = p
+    hc = np.zeros((12, nz + 2, ny + 2, pitch), dtype=np.float32)
+    hc[..., : nx + 2] = coef
+    dc = torch.from_numpy(hc).cuda()
+    ptrs = (ctypes.c_void_p * 12)(*[dc[k].data_ptr() for k in range(12)])
+    a = torch.from_numpy(hp).cuda()
+    b = a.clone()
+    g = torch.zeros(max(iters, 1), dtype=torch.float64, device="cuda")
+    ci = ctypes.c_int(-1)
+    if form == 0:
+        gb.call("appfis_gb_himeno", ptrs, a.data_ptr(), b.data_ptr(), nx, ny, nz, pitch, iters, omega, g.data_ptr(),
+                ctypes.byref(ci), None)
+    else:
+        half = torch.empty(13 * hp.size, dtype=torch.float16, device="cuda")
+        gb.call("appfis_gb_himeno_mixed", ptrs, a.data_ptr(), b.data_ptr(), half.data_ptr(), nx, ny, nz, pitch, iters,
+                period, omega, g.data_ptr(), ctypes.byref(ci), None)
+    gb.call("appfis_gb_stream_sync", None)
+    out = (a if ci.value == 0 else b).cpu().numpy()[:, :, : nx + 2]
+    return out, g.cpu().numpy()[:iters]
+
+
+# 16-byte aligned rows select the TMA-staged kernels: ragged x tiles (the first tile starts at the
+# ghost column), y not a multiple of 8, z chunks of unequal length, tiny grids
+@pytest.mark.parametrize("nx,ny,nz,pitch,iters", [(1, 1, 1, 8, 3), (30, 7, 5, 32, 4), (31, 9, 33, 40, 5),
+                                                  (64, 17, 70, 72, 3), (95, 8, 64, 104, 2)])
+def test_tma_plain_bit_exact(gb, torch_cuda, nx, ny, nz, pitch, iters):
+    coef = W.himeno_coef(nx, ny, nz, seed=3 * nx + ny)
+    p = W.himeno_p(nx, ny, nz)
+    p[1:-1, 1:-1, 1:-1] += W.uniform(5, nx * ny * nz).reshape(nz, ny, nx).astype(np.float32)
+    out, gosa = device_run(gb, torch_cuda, coef, p, iters, pitch)
+    ref, rgosa = O.himeno(coef, p, iters, 0.8)
+    assert np.array_equal(out, ref)
+    np.testing.assert_allclose(gosa, rgosa, rtol=1e-12)
+
+
+def test_tma_and_dense_rows_agree(gb, torch_cuda):
+    """The same sweep on dense rows (register-prefetch kernel) and on padded rows (TMA kernel)."""
+    nx, ny, nz, iters = 45, 19, 37, 4
+    coef = W.himeno_coef(nx, ny, nz, seed=11)
+    p = W.himeno_p(nx, ny, nz)
+    dense, gd = device_run(gb, torch_cuda, coef, p, iters, nx + 2)   # 47: not 16-byte rows
+    padded, gp = device_run(gb, torch_cuda, coef, p, iters, 48)
+    assert np.array_equal(dense, padded)
+    np.testing.assert_allclose(gd, gp, rtol=1e-12)
+
+
+@pytest.mark.parametrize("pitch", [67, 72])  # register-prefetch kernel, TMA kernel
+def test_mixed_error_both_kernels(gb, torch_cuda, pitch):
+    """FP16 defect correction on both inner-sweep kernels: p within 2.5e-4 of the FP64 oracle,
+    gosa within 1% per sweep."""
+    nx, ny, nz, iters = 65, 33, 47, 40
+    p64, g64 = O.himeno(W.himeno_coef(nx, ny, nz, dtype=np.float64), W.himeno_p(nx, ny, nz, dtype=np.float64), iters, 0.8,
+                        dtype=np.float64)
+    mixed, gm = device_run(gb, torch_cuda, W.himeno_coef(nx, ny, nz), W.himeno_p(nx, ny, nz), iters, pitch, form=1)
+    assert np.abs(mixed - p64).max() < 2.5e-4
+    np.testing.assert_allclose(gm, g64, rtol=1e-2)

@@ -41,9 +41,11 @@ def test_golden_reference_form(gb, torch_cuda, f):
 @pytest.mark.parametrize("nx,ny,nz,iters,ry,kz,pitch", [(1, 1, 1, 2, 0, 0, None), (37, 29, 11, 3, 4, 0, None),
                                                         (64, 70, 33, 2, 2, 16, 80), (33, 17, 130, 2, 4, 64, None),
                                                         (100, 3, 5, 4, 2, 3, 112),
-                                                        # vectorised tile (16-byte rows): aligned, ragged x, ragged y/z
+                                                        # TMA-staged tile (16-byte rows): aligned, ragged x, ragged y/z,
+                                                        # short z chunks, a single plane
                                                         (64, 70, 33, 2, 0, 16, 72), (37, 29, 11, 3, 0, 0, 48),
-                                                        (130, 17, 21, 2, 0, 8, 140), (4, 1, 2, 3, 0, 0, 12)])
+                                                        (130, 17, 21, 2, 0, 8, 140), (4, 1, 2, 3, 0, 0, 12),
+                                                        (70, 35, 19, 3, 0, 5, 80), (9, 16, 1, 2, 0, 0, 20)])
 def test_reference_form_vs_oracle(gb, torch_cuda, nx, ny, nz, iters, ry, kz, pitch):
     f = W.fdtd_padded(nx, ny, nz, nx * ny + nz)
     out = run(gb, torch_cuda, f, iters, 0, 0.1, pitch=pitch, ry=ry, kz=kz)
@@ -61,8 +63,9 @@ def test_weighted_form_vs_oracle(gb, torch_cuda):
     assert np.all(out[:4] == 0) and np.all(out[..., :4] == 0)  # halo untouched
 
 
-@pytest.mark.parametrize("pitch,ry", [(None, 2), (72, 0)])
-def test_fp16_both_tiles_agree(gb, torch_cuda, pitch, ry):
+# scalar tile, TMA-staged tile (rows of 72 halves = 144 B), register-staged vector tile (76 halves)
+@pytest.mark.parametrize("pitch,ry", [(None, 2), (72, 0), (76, 0)])
+def test_fp16_tiles_agree(gb, torch_cuda, pitch, ry):
     w = W.fdtd_weights()
     f = W.fdtd_padded(64, 40, 24, 13)
     a = run(gb, torch_cuda, f, 6, 1, weights=w, dtype="f16", pitch=pitch, ry=ry)
@@ -80,3 +83,12 @@ def test_fp16_storage_error(gb, torch_cuda):
     o16 = run(gb, torch_cuda, f, 50, 1, weights=w, dtype="f16")
     assert np.abs(o32 - ref64).max() < 1e-5
     assert np.abs(o16 - ref64).max() < 2e-3
+
+
+def test_fp16_tma_and_vector_tiles_agree(gb, torch_cuda):
+    """Same FP32 arithmetic on FP16 storage: the TMA-staged and register-staged tiles agree."""
+    w = W.fdtd_weights()
+    f = W.fdtd_padded(61, 23, 17, 21)
+    a = run(gb, torch_cuda, f, 4, 1, weights=w, dtype="f16", pitch=72)
+    b = run(gb, torch_cuda, f, 4, 1, weights=w, dtype="f16", pitch=76)
+    assert np.abs(a - b).max() <= 1e-3
