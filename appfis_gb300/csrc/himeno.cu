@@ -25,6 +25,7 @@
 #include <type_traits>
 
 #include "gb_common.cuh"
+#include "f32x2.cuh"
 #include "tma.cuh"
 
 namespace {
@@ -434,10 +435,160 @@ __global__ void __launch_bounds__(RX* RY) himeno_tma(const __grid_constant__ Til
     if (k < k1) {  // a wait gave up: report, let the copies still in flight land, poison gosa
         if (t == 0) {
             atomicOr(status, (unsigned)gb::ST_TMA_TIMEOUT);
-            for (int kk = k; kk < min(k + S, k1); kk++) gb::tma::wait(&bar[(kk - k0) % S], (unsigned)((kk - k0) / S) & 1u);
+            for (int kk = k; kk < min(k + S, k1); kk++)
+                gb::tma::wait(&bar[(kk - k0) % S], (unsigned)((kk - k0) / S) & 1u, gb::tma::DRAIN_NS);
         }
     }
     if (gosa) gosa_reduce(k < k1 ? __longlong_as_double(0x7ff8000000000000ll) : g.value(), partials, ticket, gosa);
+}
+
+// ---------------------------------------------------------------- FP16 inner sweep, two points per thread
+// The defect-correction sweep is instruction-bound in the one-point form (each FP16 neighbour
+// is converted where it is read, and every point pays the loop, wait and barrier overhead), so
+// this form gives each thread an x pair and does the arithmetic with packed FP32 pair
+// instructions.  Tile 64 x 8 points (32 x 8 threads).  Per plane k a pipeline stage brings the
+// eleven FP16/FP32 per-point tiles of plane k (a0 a1 a2 b0 b1 b2 c0 c1 c2 bnd as FP16, a3 as
+// FP32, D as FP16) and the FP16 box of e plane k+2 (80 x 10, x origin = tile x - 8).  The threads
+// convert that box once into an FP32 ring slot (planes k-1 .. k+2 resident), so the 19 neighbour
+// reads of a pair are 19 FP32 shared loads (paired where the pair's columns are contiguous).
+constexpr int MX = 64, MY = 8, MXO = 8, MW = MX + 2 * MXO;
+constexpr int MEB = MW * (MY + 2) * 2;                  // FP16 e box bytes (1600)
+constexpr int MES = (MEB + 127) / 128 * 128;            // its slot
+constexpr int MCT = 10 * MX * MY * 2 + MX * MY * 4 + MX * MY * 2;  // per-point tiles of a plane (13312)
+constexpr int MSTG = MCT + MES;                         // one stage
+constexpr int MR32 = MW * (MY + 2);                     // floats per FP32 ring slot
+constexpr int MIX_S = 3;
+constexpr int mixed2_smem(int S) { return S * MSTG + 4 * MR32 * 4 + 3 * MES + S * 8; }
+
+__device__ __forceinline__ void e_box_to_f32(const unsigned char* src, float* dst, int t)
+{
+    const __half2* h = reinterpret_cast<const __half2*>(src);
+    float2* d = reinterpret_cast<float2*>(dst);
+    for (int q = t; q < MR32 / 2; q += MX / 2 * MY) d[q] = __half22float2(h[q]);
+}
+
+template <int S>
+__global__ void __launch_bounds__(MX / 2 * MY) himeno_mixed2(const __grid_constant__ TileMaps maps, __half* __restrict__ eout,
+                                                             int nx, int ny, int nz, int pitch, int py, int kz, float omega,
+                                                             float inv_omega, double* __restrict__ partials,
+                                                             unsigned* __restrict__ ticket, double* __restrict__ gosa,
+                                                             unsigned* __restrict__ status)
+{
+    namespace f2 = gb::f2;
+    extern __shared__ __align__(128) unsigned char tsm[];
+    unsigned char* stages = tsm;
+    float* ring = reinterpret_cast<float*>(tsm + S * MSTG);
+    unsigned char* pro = tsm + S * MSTG + 4 * MR32 * 4;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(pro + 3 * MES);
+    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * (MX / 2) + tx;
+    const int x0 = blockIdx.x * MX, y0 = 1 + blockIdx.y * MY;
+    const int xa = x0 + 2 * tx, j = y0 + ty;
+    const int k0 = 1 + blockIdx.z * kz, k1 = min(k0 + kz, nz + 1);
+    const bool acta = xa >= 1 && xa <= nx && j <= ny, actb = xa + 1 <= nx && j <= ny;
+    if (gb::tma::smem_u32(tsm) & 127u) {
+        if (t == 0) atomicOr(status, (unsigned)gb::ST_SMEM_ALIGN);
+        if (gosa) gosa_reduce(__longlong_as_double(0x7ff8000000000000ll), partials, ticket, gosa);
+        return;
+    }
+    if (t == 0) {
+#pragma unroll
+        for (int s = 0; s < S; s++) gb::tma::bar_init(&bar[s], 1);
+        gb::tma::fence_init();
+        for (int n = 0; n < 13; n++) gb::tma::prefetch_map(&maps.m[n]);
+    }
+    __syncthreads();
+    auto slot = [&](int pl) { return ring + ((pl - (k0 - 1)) & 3) * MR32; };
+    auto issue = [&](int k) {
+        const int s = (k - k0) % S;
+        unsigned char* st = stages + s * MSTG;
+        gb::tma::arrive_expect(&bar[s], MCT + MEB * (k == k0 ? 4 : 1));
+        if (k == k0)
+            for (int d = 0; d < 3; d++) gb::tma::load_3d(pro + d * MES, &maps.m[12], x0 - MXO, y0 - 1, k0 - 1 + d, &bar[s]);
+#pragma unroll
+        for (int n = 0; n < 10; n++) gb::tma::load_3d(st + n * MX * MY * 2, &maps.m[n], x0, y0, k, &bar[s]);
+        gb::tma::load_3d(st + 10 * MX * MY * 2, &maps.m[10], x0, y0, k, &bar[s]);
+        gb::tma::load_3d(st + 10 * MX * MY * 2 + MX * MY * 4, &maps.m[11], x0, y0, k, &bar[s]);
+        gb::tma::load_3d(st + MCT, &maps.m[12], x0 - MXO, y0 - 1, k + 2, &bar[s]);
+    };
+    if (t == 0)
+        for (int k = k0; k < min(k0 + S, k1); k++) issue(k);
+
+    float2 g = make_float2(0.0f, 0.0f);
+    bool bad = false;
+    int k = k0;
+    const int cq = ty * MX + 2 * tx;          // this pair in a per-point tile (elements)
+    const int q = (ty + 1) * MW + 2 * tx + MXO;  // this pair in a ring slot
+    const float2 wsplat = f2::splat(omega), isplat = f2::splat(inv_omega);
+    for (; k < k1; k++) {
+        const int s = (k - k0) % S;
+        if (!gb::tma::wait(&bar[s], (unsigned)((k - k0) / S) & 1u)) bad = true;
+        const unsigned char* st = stages + s * MSTG;
+        if (k == k0) {  // uniform
+            for (int d = 0; d < 3; d++) e_box_to_f32(pro + d * MES, slot(k0 - 1 + d), t);
+            __syncthreads();
+        }
+        e_box_to_f32(st + MCT, slot(k + 2), t);  // plane k+2 into the slot plane k-2 left
+        {
+            const float* sm = slot(k - 1);
+            const float* s0 = slot(k);
+            const float* sp = slot(k + 1);
+            auto c2 = [&](const float* b, int dy) { return *reinterpret_cast<const float2*>(b + q + dy * MW); };
+            auto lf = [&](const float* b, int dy) { return b[q + dy * MW - 1]; };
+            auto rt = [&](const float* b, int dy) { return b[q + dy * MW + 2]; };
+            // rows with x neighbours: (dy, dz) = (0,0) (1,0) (-1,0) (0,1) (0,-1)
+            const float2 e0 = c2(s0, 0), yp = c2(s0, 1), ym = c2(s0, -1), zp = c2(sp, 0), zm = c2(sm, 0);
+            const float e0l = lf(s0, 0), e0r = rt(s0, 0), ypl = lf(s0, 1), ypr = rt(s0, 1), yml = lf(s0, -1), ymr = rt(s0, -1);
+            const float zpl = lf(sp, 0), zpr = rt(sp, 0), zml = lf(sm, 0), zmr = rt(sm, 0);
+            // diagonal rows (dy, dz) = (+-1, +-1): centre pair only
+            const float2 ypzp = c2(sp, 1), ymzp = c2(sp, -1), ypzm = c2(sm, 1), ymzm = c2(sm, -1);
+            // F(+1, dy, dz) = (centre.y, right), F(-1, dy, dz) = (left, centre.x)
+            const float2 xp = make_float2(e0.y, e0r), xm = make_float2(e0l, e0.x);
+            const float2 xpyp = make_float2(yp.y, ypr), xmyp = make_float2(ypl, yp.x);
+            const float2 xpym = make_float2(ym.y, ymr), xmym = make_float2(yml, ym.x);
+            const float2 xpzp = make_float2(zp.y, zpr), xmzp = make_float2(zpl, zp.x);
+            const float2 xpzm = make_float2(zm.y, zmr), xmzm = make_float2(zml, zm.x);
+            float2 co[10];
+#pragma unroll
+            for (int n = 0; n < 10; n++) co[n] = __half22float2(reinterpret_cast<const __half2*>(st + n * MX * MY * 2)[cq / 2]);
+            const float2 a3 = reinterpret_cast<const float2*>(st + 10 * MX * MY * 2)[cq / 2];
+            const float2 D = __half22float2(reinterpret_cast<const __half2*>(st + 10 * MX * MY * 2 + MX * MY * 4)[cq / 2]);
+            // a0 a1 a2 b0 b1 b2 c0 c1 c2 bnd
+            float2 ne = f2::mul(co[0], xp);
+            ne = f2::fma(co[1], yp, ne);
+            ne = f2::fma(co[2], zp, ne);
+            ne = f2::fma(co[3], f2::sub(f2::sub(xpyp, xpym), f2::sub(xmyp, xmym)), ne);
+            ne = f2::fma(co[4], f2::sub(f2::sub(ypzp, ymzp), f2::sub(ypzm, ymzm)), ne);
+            ne = f2::fma(co[5], f2::sub(f2::sub(xpzp, xmzp), f2::sub(xpzm, xmzm)), ne);
+            ne = f2::fma(co[6], xm, ne);
+            ne = f2::fma(co[7], ym, ne);
+            ne = f2::fma(co[8], zm, ne);
+            const float2 v = f2::add(f2::fma(f2::mul(wsplat, co[9]), f2::sub(f2::mul(a3, ne), e0), e0), D);
+            float2 ss = f2::mul(f2::sub(v, e0), isplat);
+            const size_t cc = ((size_t)k * py + j) * pitch + xa;
+            const __half2 hv = __float22half2_rn(v);
+            if (!bad) {
+                if (acta && actb) {
+                    *reinterpret_cast<__half2*>(eout + cc) = hv;
+                } else {
+                    if (acta) eout[cc] = __low2half(hv);
+                    if (actb) eout[cc + 1] = __high2half(hv);
+                }
+            }
+            ss.x = acta ? ss.x : 0.0f;
+            ss.y = actb ? ss.y : 0.0f;
+            g = f2::fma(ss, ss, g);
+        }
+        // everyone is done with stage s, the slot of plane k-1 and the conversions of plane k+2
+        if (__syncthreads_or(bad)) break;
+        if (t == 0 && k + S < k1) issue(k + S);
+    }
+    if (k < k1 && t == 0) {  // a wait gave up: report and let the copies still in flight land
+        atomicOr(status, (unsigned)gb::ST_TMA_TIMEOUT);
+        for (int kk = k; kk < min(k + S, k1); kk++)
+                gb::tma::wait(&bar[(kk - k0) % S], (unsigned)((kk - k0) / S) & 1u, gb::tma::DRAIN_NS);
+    }
+    if (gosa)
+        gosa_reduce(k < k1 ? __longlong_as_double(0x7ff8000000000000ll) : (double)g.x + (double)g.y, partials, ticket, gosa);
 }
 
 // z planes per CTA: about HKZ, balanced so that no chunk is much shorter than the others
@@ -448,7 +599,7 @@ inline int balanced_kz(int nz, int target)
 }
 
 constexpr int HBX = 32, HBY = 4, HKZ = 32;
-constexpr int TMA_S_PLAIN = 3, TMA_S_MIXED = 4;
+constexpr int TMA_S_PLAIN = 3;
 
 // Tensor maps of the plain form: the 12 FP32 coefficient fields and the iterated p buffer.
 int plain_maps(const float* const* coef, const float* pin, int nx, int ny, int nz, int pitch, TileMaps* m)
@@ -566,25 +717,26 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     himeno_half_coef<<<dim3(gb::ceil_div(nx, 128), ny, nz), 128, 0, st>>>(cf, Hc, field, nx, ny, nz, pitch, ny + 2);
     dim3 blk(HBX, HBY), grd(gb::ceil_div(nx, HBX), gb::ceil_div(ny, HBY), gb::ceil_div(nz, HKZ));
     dim3 rblk(RX, RY), rgrd(gb::ceil_div(nx, RX), gb::ceil_div(ny, RY), gb::ceil_div(nz, HKZ));
-    // TMA-staged inner sweeps when the FP16 rows are 16-byte aligned (pitch a multiple of 8)
+    // TMA-staged inner sweeps (two points per thread) when the FP16 rows are 16-byte aligned
+    // (pitch a multiple of 8)
     const bool use_tma = pitch % 8 == 0 && gb::aligned16(hw) && gb::aligned16(coef[3]);
     const int tkz = balanced_kz(nz, HKZ);
-    dim3 tgrd(nx / RX + 1, gb::ceil_div(ny, RY), gb::ceil_div(nz, tkz));
+    dim3 tblk(MX / 2, MY), tgrd(nx / MX + 1, gb::ceil_div(ny, MY), gb::ceil_div(nz, tkz));
     TileMaps tmaps[2];
     unsigned* status = nullptr;
-    constexpr int tsmem = TmaLayout<1>::smem(TMA_S_MIXED);
+    constexpr int tsmem = mixed2_smem(MIX_S);
     if (use_tma) {
         const int py = ny + 2;
         for (int n = 0; n < 10; n++)
-            GB_TRY(gb::tensor_map_3d(&tmaps[0].m[n], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, hf.c[n], nx + 2, py, nz + 2, pitch, py, RX, RY));
-        GB_TRY(gb::tensor_map_3d(&tmaps[0].m[10], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, coef[3], nx + 2, py, nz + 2, pitch, py, RX, RY));
-        GB_TRY(gb::tensor_map_3d(&tmaps[0].m[11], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, Dd, nx + 2, py, nz + 2, pitch, py, RX, RY));
+            GB_TRY(gb::tensor_map_3d(&tmaps[0].m[n], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, hf.c[n], nx + 2, py, nz + 2, pitch, py, MX, MY));
+        GB_TRY(gb::tensor_map_3d(&tmaps[0].m[10], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, coef[3], nx + 2, py, nz + 2, pitch, py, MX, MY));
+        GB_TRY(gb::tensor_map_3d(&tmaps[0].m[11], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, Dd, nx + 2, py, nz + 2, pitch, py, MX, MY));
         tmaps[1] = tmaps[0];
         for (int b = 0; b < 2; b++)
-            GB_TRY(gb::tensor_map_3d(&tmaps[b].m[12], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, E[b], nx + 2, py, nz + 2, pitch, py,
-                                     TmaLayout<1>::W, RY + 2));
+            GB_TRY(gb::tensor_map_3d(&tmaps[b].m[12], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, E[b], nx + 2, py, nz + 2, pitch, py, MW,
+                                     MY + 2));
         GB_TRY(gb::status_word(&status));
-        GB_CUDA(cudaFuncSetAttribute(himeno_tma<1, TMA_S_MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem));
+        GB_CUDA(cudaFuncSetAttribute(himeno_mixed2<MIX_S>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem));
     }
     double* rpartials = nullptr;
     unsigned* rticket = nullptr;
@@ -598,9 +750,8 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     const float inv_omega = 1.0f / omega;
     for (int it = 0; it < iters; it++) {
         if (use_tma)
-            himeno_tma<1, TMA_S_MIXED><<<tgrd, rblk, tsmem, st>>>(tmaps[ec], E[1 - ec], nx, ny, nz, pitch, ny + 2, tkz, omega,
-                                                                 inv_omega, rpartials, rticket,
-                                                                 dev_gosa ? dev_gosa + it : nullptr, status);
+            himeno_mixed2<MIX_S><<<tgrd, tblk, tsmem, st>>>(tmaps[ec], E[1 - ec], nx, ny, nz, pitch, ny + 2, tkz, omega, inv_omega,
+                                                           rpartials, rticket, dev_gosa ? dev_gosa + it : nullptr, status);
         else
             himeno_ring<1><<<rgrd, rblk, 0, st>>>(cf, hf, E[ec], E[1 - ec], Dd, nx, ny, nz, pitch, ny + 2, HKZ, omega, inv_omega,
                                                   rpartials, rticket, dev_gosa ? dev_gosa + it : nullptr);

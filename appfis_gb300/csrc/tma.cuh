@@ -71,13 +71,16 @@ __device__ __forceinline__ void prefetch_map(const CUtensorMap* map)
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
 
+// Tests the phase; a thread whose phase is not complete is suspended (up to ~0.5 ms, woken
+// early when the phase completes), so waiting warps do not spin on the issue slots that the
+// working warps need.
 __device__ __forceinline__ bool try_wait(uint64_t* bar, unsigned parity)
 {
     uint32_t ok;
     asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n}"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(500000u)
         : "memory");
     return ok != 0;
 }
@@ -89,15 +92,16 @@ __device__ __forceinline__ uint64_t global_ns()
     return t;
 }
 
-// Waits for the phase with `parity` of `bar` to complete; gives up after about one second
-// (or 2^24 polls) and returns false.
-__device__ __forceinline__ bool wait(uint64_t* bar, unsigned parity)
+// Waits for the phase with `parity` of `bar` to complete; gives up after `limit_ns` of wall
+// clock (default one second; at most 2^22 tests) and returns false.
+constexpr uint64_t DRAIN_NS = 10000000ull;  // 10 ms: waits for copies in flight after a failure
+__device__ __forceinline__ bool wait(uint64_t* bar, unsigned parity, uint64_t limit_ns = 1000000000ull)
 {
     if (try_wait(bar, parity)) return true;
     const uint64_t t0 = global_ns();
-    for (unsigned n = 0; n < (1u << 24); n++) {
+    for (unsigned n = 0; n < (1u << 22); n++) {
         if (try_wait(bar, parity)) return true;
-        if ((n & 255u) == 255u && global_ns() - t0 > 1000000000ull) break;
+        if (global_ns() - t0 > limit_ns) break;
     }
     return false;
 }

@@ -1,0 +1,119 @@
+"""The reference's five sample applications, UNCHANGED, built against the drop-in headers and
+run on the GPU, against the same sources built with the reference's own headers (APPFIS_CPU,
+OpenMP, the single-rank MPI stand-in) and run on the host: the values each application prints
+with -output must agree — HeatDiffusion Max/Min (FP64) and GameOfLife Live Count identical,
+Himeno Sum within 2e-4 relative (the reference sums FP32 values in an FP32 accumulator, so its own
+result moves by ~1e-4 with the OpenMP thread count; the engine sums in double) — and
+the Triton flood application, run on a synthetic case through its own readers (key=value
+configuration, ASCII DEM with its 6-line header, initial depth file, point source with a
+hydrograph), must write the same h/u/v fields (6 decimals, the applications' output format).
+
+Needs oracle/_ref/apps/ (flattened from the reference tree by oracle/build_ref.py)."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from appfis_gb300 import workloads as W
+from oracle import build_ref
+from tests.dropin import build_apps
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not build_apps.available(), reason="application sources not present")]
+
+
+@pytest.fixture(scope="module")
+def exes(gb):
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=len(build_apps.APPS)) as ex:
+        refs = ex.map(build_ref.app_ref_exe, build_apps.APPS)
+        gbx = build_apps.build()
+        ref = dict(zip(build_apps.APPS, refs))
+    return gbx, ref
+
+
+def run(exe, args, cwd):
+    r = subprocess.run([exe] + args, capture_output=True, text=True, timeout=600, cwd=cwd)
+    assert r.returncode == 0, (exe, r.stdout[-2000:], r.stderr[-2000:])
+    return r.stdout
+
+
+def values(out, keys):
+    got = {}
+    for k in keys:
+        m = re.search(r"^%s:\s*(\S+)\s*$" % re.escape(k), out, re.M)
+        assert m, (k, out)
+        got[k] = m.group(1)
+    return got
+
+
+@pytest.mark.parametrize("app,args,keys,rtol", [
+    ("HeatDiffusion", ["-dimx=48", "-dimy=40", "-dimz=36", "-iteration=20"], ["Max", "Min"], 0),
+    ("HeatDiffusion", ["-dimx=33", "-dimy=17", "-dimz=9", "-iteration=7"], ["Max", "Min"], 0),
+    ("GameOfLife", ["-dimx=300", "-dimy=200", "-iteration=50"], ["Live Count"], 0),
+    ("GameOfLife", ["-dimx=67", "-dimy=45", "-iteration=31"], ["Live Count"], 0),
+    ("Himeno", ["-dimx=65", "-dimy=65", "-dimz=129", "-iteration=20"], ["Sum"], 2e-4),
+    ("Himeno", ["-dimx=33", "-dimy=17", "-dimz=20", "-iteration=5"], ["Sum"], 2e-4),
+])
+def test_application_outputs_match(exes, tmp_path, app, args, keys, rtol):
+    gbx, ref = exes
+    a = values(run(gbx[app], args + ["-output"], str(tmp_path)), keys)
+    b = values(run(ref[app], args + ["-output", "-thread=4"], str(tmp_path)), keys)
+    if rtol == 0:
+        assert a == b
+    else:
+        for k in keys:
+            assert float(a[k]) == pytest.approx(float(b[k]), rel=rtol), (k, a[k], b[k])
+
+
+def test_fdtd_application_runs(exes, tmp_path):
+    """FDTD3d prints no field values; it must run to completion and report its rate."""
+    gbx, _ = exes
+    out = run(gbx["FDTD3d"], ["-dimx=64", "-dimy=48", "-dimz=40", "-iteration=10", "-output"], str(tmp_path))
+    assert re.search(r"^GFLOPS:\s*\S+", out, re.M)
+
+
+def _write_grid(path, a, header=""):
+    with open(path, "w") as f:
+        f.write(header)
+        for row in a:
+            f.write(" ".join("%.6f" % v for v in row) + "\n")
+
+
+def _triton_case(d, nx, ny, seed, duration):
+    dem, h = W.triton_domain(ny, nx, seed)
+    _write_grid(os.path.join(d, "dem.asc"), dem,
+                "ncols %d\nnrows %d\nxllcorner 0.0\nyllcorner 0.0\ncellsize 10.0\nNODATA_value -9999\n" % (nx, ny))
+    _write_grid(os.path.join(d, "h.asc"), h)
+    with open(os.path.join(d, "hydro.txt"), "w") as f:
+        f.write("% time (hr), flow (m3/s)\n0, 0\n0.01, 8.0\n0.03, 3.0\n1.0, 0.0\n")
+    with open(os.path.join(d, "src.txt"), "w") as f:
+        f.write("%% x, y\n%.1f, %.1f\n" % (10.0 * (nx // 2) - 5.0, 10.0 * (ny // 2) - 5.0))
+    cfg = dict(dem_filename="dem.asc", h_infile="h.asc", hydrograph_filename="hydro.txt", src_loc_file="src.txt",
+               num_sources=1, const_mann=0.035, time_step=1.0, time_increment_fixed=0, time_series_flag=0, courant=0.5,
+               hextra=0.001, gpu_direct_flag=0, num_runoffs=0, num_extbc=0, print_option="h", input_format="ASC",
+               output_format="ASC", output_option="SEQ", sim_start_time=0, sim_duration=duration, print_interval=60)
+    with open(os.path.join(d, "case.cfg"), "w") as f:
+        f.write("".join("%s=%s\n" % kv for kv in cfg.items()))
+
+
+@pytest.mark.parametrize("nx,ny,seed,duration", [(48, 40, 77, 120), (97, 61, 5, 90)])
+def test_triton_application_case_files(exes, tmp_path, nx, ny, seed, duration):
+    gbx, ref = exes
+    out = {}
+    for name, exe, extra in (("gb", gbx["Triton"], []), ("ref", ref["Triton"], ["-thread=4"])):
+        d = tmp_path / name
+        d.mkdir()
+        _triton_case(str(d), nx, ny, seed, duration)
+        text = run(exe, ["case.cfg", "-output"] + extra, str(d))
+        steps = int(re.search(r"^Number of iteration:\s*(\d+)", text, re.M).group(1))
+        fields = [np.loadtxt(str(d / "output" / f)) for f in ("h.txt", "u.txt", "v.txt")]
+        out[name] = (steps, fields)
+    assert out["gb"][0] == out["ref"][0]
+    h0 = W.triton_domain(ny, nx, seed)[1]
+    assert out["ref"][1][0].sum() > h0.sum()  # the point source added water
+    for a, b in zip(out["gb"][1], out["ref"][1]):
+        assert a.shape == (ny, nx)
+        # 6 printed decimals; cbrt/sqrt may differ in the last bit between the CUDA and host libraries
+        assert np.abs(a - b).max() <= 2e-6
