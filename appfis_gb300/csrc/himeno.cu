@@ -457,7 +457,7 @@ constexpr int MES = (MEB + 127) / 128 * 128;            // its slot
 constexpr int MCT = 10 * MX * MY * 2 + MX * MY * 4 + MX * MY * 2;  // per-point tiles of a plane (13312)
 constexpr int MSTG = MCT + MES;                         // one stage
 constexpr int MR32 = MW * (MY + 2);                     // floats per FP32 ring slot
-constexpr int MIX_S = 3;
+constexpr int MIX_S = 2;
 constexpr int mixed2_smem(int S) { return S * MSTG + 4 * MR32 * 4 + 3 * MES + S * 8; }
 
 __device__ __forceinline__ void e_box_to_f32(const unsigned char* src, float* dst, int t)

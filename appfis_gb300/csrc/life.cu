@@ -258,14 +258,14 @@ constexpr int TB_STEPS = 16;  // generations per launch (max)
 constexpr int TB_WARPS = 8;
 constexpr int TB_RR = TB_ROWS + 2 * TB_STEPS;
 
-// Row summary of one word for the bit-sliced neighbour count; lanes 0 / 31 see 0 beyond the tile
-// (their outer bits are the stale halo, never read by output words).
+// Row summary of one word for the bit-sliced neighbour count.  Lanes 0 / 31 get their own word
+// back from the shuffles, so their outer bit is wrong; those lanes are the stale halo, whose
+// wrong bits travel one cell per generation and never reach an output word.
 __device__ __forceinline__ RowBits tile_row(uint32_t w, int lane)
 {
-    uint32_t lw = __shfl_up_sync(FULL, w, 1);
-    uint32_t rw = __shfl_down_sync(FULL, w, 1);
-    if (lane == 0) lw = 0u;
-    if (lane == 31) rw = 0u;
+    (void)lane;
+    const uint32_t lw = __shfl_up_sync(FULL, w, 1);
+    const uint32_t rw = __shfl_down_sync(FULL, w, 1);
     const uint32_t L = __funnelshift_l(lw, w, 1), R = __funnelshift_r(w, rw, 1);
     RowBits r;
     r.w = w;
@@ -276,6 +276,8 @@ __device__ __forceinline__ RowBits tile_row(uint32_t w, int lane)
     return r;
 }
 
+// Count bits r0..r2 of up + mid + dn (the count-8 bit is not formed: with it dropped a count of
+// 8 reads as 0, and both rules treat 0 and 8 alike — no birth, no survival).
 template <int RULE>
 __device__ __forceinline__ uint32_t life_combine(const RowBits& up, const RowBits& mid, const RowBits& dn, uint32_t o)
 {
@@ -283,8 +285,15 @@ __device__ __forceinline__ uint32_t life_combine(const RowBits& up, const RowBit
     const uint32_t t1 = up.a1 ^ mid.h1 ^ c0, t2 = (up.a1 & mid.h1) | (c0 & (up.a1 ^ mid.h1));
     const uint32_t r0 = t0 ^ dn.a0, k0 = t0 & dn.a0;
     const uint32_t r1 = t1 ^ dn.a1 ^ k0, k1 = (t1 & dn.a1) | (k0 & (t1 ^ dn.a1));
-    const uint32_t r2 = t2 ^ k1, r3 = t2 & k1;
-    return rule_bits<RULE>(r0, r1, r2, r3, mid.w, o);
+    const uint32_t r2 = t2 ^ k1;
+    const uint32_t c = mid.w;
+    if (RULE == APPFIS_GB_LIFE_REFERENCE) {
+        const uint32_t birth = r0 & r1 & ~r2;                      // count 3
+        const uint32_t keep = (~r2 & r1) | (r2 & ~r1 & ~r0);       // count 2, 3, 4
+        return (c & keep & o) | (~c & (birth | o));
+    } else {
+        return r1 & ~r2 & (r0 | c);                                // count 3, or count 2 and alive
+    }
 }
 
 template <int RULE>

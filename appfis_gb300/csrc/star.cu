@@ -20,6 +20,7 @@
 #include <cuda_fp16.h>
 
 #include "gb_common.cuh"
+#include "f32x2.cuh"
 #include "tma.cuh"
 
 namespace {
@@ -188,6 +189,8 @@ template <> struct Vec4<__half> {
 };
 
 __device__ __forceinline__ float f4(const float4& v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w)); }
+// lanes (c, c+1) of v, c = 0 or 2
+__device__ __forceinline__ float2 pair(const float4& v, int c) { return c == 0 ? make_float2(v.x, v.y) : make_float2(v.z, v.w); }
 
 template <class T, int MODE>
 __global__ void __launch_bounds__(256) star_r4_vec(const T* __restrict__ in, T* __restrict__ out, int nx, int ny, int nz, int px,
@@ -298,51 +301,92 @@ __global__ void __launch_bounds__(256) star_r4_vec(const T* __restrict__ in, T* 
 }
 
 // ---------------------------------------------------------------- TMA-staged form
-// A 64 x 16 (x, y) tile per CTA; each thread owns 4 consecutive x points of RYT consecutive
-// rows, and every plane is moved by the tensor memory accelerator: plane pl arrives as one
-// 72 x 24 box (the x/y halo included; the box x origin is the tile's first ghost column, a
-// 64-point boundary of the padded row, so every copy starts 16-byte aligned) in slot
-// (pl - k0 + 4) % TNS of a shared ring, signalled on that slot's mbarrier.  Thread 0 keeps
-// TNS - 5 planes in flight beyond the newest one in use.  Each thread pushes its centre values
-// of plane k+4 into its z queue (registers); the x/y windows of plane k come from the ring, except
-// the thread's own rows, which are the queue's centre entries.  With RYT = 2 a thread reads 14
-// 16-byte shared vectors per 8 points (2 queue pushes, 2 x 2 x-windows, 8 y-window rows) instead
-// of 12 per 4.  Global traffic: each plane read once per CTA (plus the 8-plane z-chunk overlap),
-// each result written once.
-constexpr int TNS = 8;                   // ring slots: planes k..k+4 resident, 3 more in flight
-constexpr int TSW = VTX + 2 * R, TSH = VTY + 2 * R;
-constexpr int TRY = 2;                   // rows per thread
+// A (16*VXT) x 16 (x, y) tile per CTA of 16 x 8 threads; each thread owns VXT consecutive x
+// points (4 or 2) of RYT = 2 consecutive rows, and every plane is moved by the tensor memory
+// accelerator: plane pl arrives as one (16*VXT + 8) x 24 box (the x/y halo included; the box x
+// origin is the tile's first ghost column, a 16*VXT-point boundary of the padded row, so every
+// copy starts 16-byte aligned) in slot (pl - k0 + 4) % TNS of a shared ring, signalled on that
+// slot's mbarrier.  Thread 0 keeps TNS - 5 planes in flight beyond the newest one in use.  Each
+// thread pushes its centre values of plane k+4 into its z queue (registers); the x/y windows of
+// plane k come from the ring, except the thread's own rows, which are the queue's centre
+// entries.  The arithmetic runs on x pairs with packed FP32-pair instructions.  VXT = 4 reads
+// 16-byte shared vectors (fewer shared-memory wavefronts); VXT = 2 halves the queue registers
+// (twice the resident warps).  Global traffic: each plane read once per CTA (plus the 8-plane
+// z-chunk overlap), each result written once.
+constexpr int TNS = 8;   // ring slots: planes k..k+4 resident, 3 more in flight
+constexpr int TRY = 2;   // rows per thread
+constexpr int TTY = 16;  // tile rows (8 thread rows x TRY)
 
-template <class T>
+template <class T, int VXT>
 struct TmaStar {
-    static constexpr int BOX = TSW * TSH * (int)sizeof(T);  // bytes per plane box
+    static constexpr int TX = 16 * VXT;             // tile x points
+    static constexpr int SW = TX + 2 * R, SH = TTY + 2 * R;
+    static constexpr int BOX = SW * SH * (int)sizeof(T);  // bytes per plane box
     static constexpr int SLOT = (BOX + 127) / 128 * 128;
     static constexpr int smem() { return TNS * SLOT + TNS * 8; }
 };
 
-template <class T> __device__ __forceinline__ float4 lds4(const T* p);
-template <> __device__ __forceinline__ float4 lds4<float>(const float* p) { return *reinterpret_cast<const float4*>(p); }
-template <> __device__ __forceinline__ float4 lds4<__half>(const __half* p)
+// VXT consecutive values, loaded from shared memory (FP32 or FP16 storage) and stored to global
+template <int VXT>
+struct VecN {
+    float v[VXT];
+};
+template <class T, int VXT> __device__ __forceinline__ VecN<VXT> ldsv(const T* p);
+template <> __device__ __forceinline__ VecN<4> ldsv<float, 4>(const float* p)
+{
+    const float4 a = *reinterpret_cast<const float4*>(p);
+    return {{a.x, a.y, a.z, a.w}};
+}
+template <> __device__ __forceinline__ VecN<2> ldsv<float, 2>(const float* p)
+{
+    const float2 a = *reinterpret_cast<const float2*>(p);
+    return {{a.x, a.y}};
+}
+template <> __device__ __forceinline__ VecN<4> ldsv<__half, 4>(const __half* p)
 {
     const uint2 u = *reinterpret_cast<const uint2*>(p);
     const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
     const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
-    return make_float4(a.x, a.y, b.x, b.y);
+    return {{a.x, a.y, b.x, b.y}};
+}
+template <> __device__ __forceinline__ VecN<2> ldsv<__half, 2>(const __half* p)
+{
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(p));
+    return {{a.x, a.y}};
+}
+template <class T, int VXT> __device__ __forceinline__ void stgv(T* p, const float* r);
+template <> __device__ __forceinline__ void stgv<float, 4>(float* p, const float* r)
+{
+    *reinterpret_cast<float4*>(p) = make_float4(r[0], r[1], r[2], r[3]);
+}
+template <> __device__ __forceinline__ void stgv<float, 2>(float* p, const float* r)
+{
+    *reinterpret_cast<float2*>(p) = make_float2(r[0], r[1]);
+}
+template <> __device__ __forceinline__ void stgv<__half, 4>(__half* p, const float* r)
+{
+    Vec4<__half>::st(p, make_float4(r[0], r[1], r[2], r[3]));
+}
+template <> __device__ __forceinline__ void stgv<__half, 2>(__half* p, const float* r)
+{
+    *reinterpret_cast<__half2*>(p) = __floats2half2_rn(r[0], r[1]);
 }
 
-template <class T, int MODE, int RYT>
-__global__ void __launch_bounds__(16 * (VTY / RYT)) star_r4_tma(const __grid_constant__ CUtensorMap map, T* __restrict__ out,
-                                                               int nx, int ny, int nz, int px, int py, int kz, float coeff,
-                                                               StarW wt, unsigned* __restrict__ status)
+template <class T, int MODE, int VXT>
+__global__ void __launch_bounds__(128, VXT == 4 ? 4 : 6) star_r4_tma(const __grid_constant__ CUtensorMap map, T* __restrict__ out,
+                                                                     int nx, int ny, int nz, int px, int py, int kz, float coeff,
+                                                                     StarW wt, unsigned* __restrict__ status)
 {
-    typedef TmaStar<T> Lay;
+    namespace f2 = gb::f2;
+    typedef TmaStar<T, VXT> Lay;
+    constexpr int SW = Lay::SW;
     extern __shared__ __align__(128) unsigned char tsm[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(tsm + TNS * Lay::SLOT);
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * 16 + tx;
-    const int bx0 = blockIdx.x * VTX, by0 = blockIdx.y * VTY;  // box origin (padded coordinates)
-    const int x = R + bx0 + VX * tx, y = R + by0 + RYT * ty;    // this thread's first point
+    const int bx0 = blockIdx.x * Lay::TX, by0 = blockIdx.y * TTY;  // box origin (padded coordinates)
+    const int x = R + bx0 + VXT * tx, y = R + by0 + TRY * ty;       // this thread's first point
     const int k0 = R + blockIdx.z * kz, k1 = min(k0 + kz, nz + R);
-    const int plast = k1 + R - 1;                               // last plane the chunk reads
+    const int plast = k1 + R - 1;                                   // last plane the chunk reads
     const size_t plane = (size_t)px * py;
     if (gb::tma::smem_u32(tsm) & 127u) {
         if (t == 0) atomicOr(status, (unsigned)gb::ST_SMEM_ALIGN);
@@ -363,18 +407,20 @@ __global__ void __launch_bounds__(16 * (VTY / RYT)) star_r4_tma(const __grid_con
         gb::tma::arrive_expect(&bar[n], Lay::BOX);
         gb::tma::load_3d(tsm + n * Lay::SLOT, &map, bx0, by0, pl, &bar[n]);
     };
-    auto ready = [&](int pl) { return gb::tma::wait(&bar[(pl - pbase) % TNS], (unsigned)((pl - pbase) / TNS) & 1u); };
+    auto ready = [&](int pl, uint64_t limit = 1000000000ull) {
+        return gb::tma::wait(&bar[(pl - pbase) % TNS], (unsigned)((pl - pbase) / TNS) & 1u, limit);
+    };
     if (t == 0)
         for (int pl = pbase; pl < pbase + TNS && pl <= plast; pl++) issue(pl);
 
-    const int own = (RYT * ty + R) * TSW + R + VX * tx;  // this thread's first row, 4 points, in a slot
+    const int own = (TRY * ty + R) * SW + R + VXT * tx;  // this thread's first row, VXT points, in a slot
     bool bad = false;
-    float4 q[RYT][9];
+    VecN<VXT> q[TRY][9];
 #pragma unroll
     for (int m = 0; m < 8; m++) {  // planes k0-4 .. k0+3
         if (!bad && !ready(pbase + m)) bad = true;
 #pragma unroll
-        for (int r = 0; r < RYT; r++) q[r][m] = lds4<T>(slot(pbase + m) + own + r * TSW);
+        for (int r = 0; r < TRY; r++) q[r][m] = ldsv<T, VXT>(slot(pbase + m) + own + r * SW);
     }
     // planes k0-4 .. k0-1 only fed the queue: their slots take planes pbase+8 .. pbase+11
     bad = __syncthreads_or(bad);
@@ -388,57 +434,82 @@ __global__ void __launch_bounds__(16 * (VTY / RYT)) star_r4_tma(const __grid_con
             if (k < k1 && !bad) {
                 if (!ready(k + R)) bad = true;
 #pragma unroll
-                for (int r = 0; r < RYT; r++) q[r][(P + 8) % 9] = lds4<T>(slot(k + R) + own + r * TSW);
+                for (int r = 0; r < TRY; r++) q[r][(P + 8) % 9] = ldsv<T, VXT>(slot(k + R) + own + r * SW);
                 const T* rowp = slot(k) + own;
-                // y-window rows m = -4..-1 and RYT..RYT+3 relative to the first row
-                float4 wv[8];
+                // y-window rows m = -4..-1 and TRY..TRY+3 relative to the first row
+                VecN<VXT> wv[8];
 #pragma unroll
                 for (int a = 1; a <= R; a++) {
-                    wv[a - 1] = lds4<T>(rowp - a * TSW);
-                    wv[R + a - 1] = lds4<T>(rowp + (RYT - 1 + a) * TSW);
+                    wv[a - 1] = ldsv<T, VXT>(rowp - a * SW);
+                    wv[R + a - 1] = ldsv<T, VXT>(rowp + (TRY - 1 + a) * SW);
                 }
 #pragma unroll
-                for (int r = 0; r < RYT; r++) {
-                    const float4 xl = lds4<T>(rowp + r * TSW - 4), xc = q[r][(P + 4) % 9], xr = lds4<T>(rowp + r * TSW + 4);
-                    const float xw[12] = {xl.x, xl.y, xl.z, xl.w, xc.x, xc.y, xc.z, xc.w, xr.x, xr.y, xr.z, xr.w};
-                    float4 ym[R], yp[R];
+                for (int r = 0; r < TRY; r++) {
+                    // x window: x-4 .. x+VXT+3 (the centre VXT values are the queue's)
+                    float xw[VXT + 2 * R];
+#pragma unroll
+                    for (int b = 0; b < R; b += VXT) {
+                        const VecN<VXT> lo = ldsv<T, VXT>(rowp + r * SW - R + b), hi = ldsv<T, VXT>(rowp + r * SW + VXT + b);
+#pragma unroll
+                        for (int e = 0; e < VXT; e++) {
+                            xw[b + e] = lo.v[e];
+                            xw[R + VXT + b + e] = hi.v[e];
+                        }
+                    }
+#pragma unroll
+                    for (int e = 0; e < VXT; e++) xw[R + e] = q[r][(P + 4) % 9].v[e];
+                    // rows relative to the first row: own rows come from the queue
+                    const VecN<VXT>* ym[R];
+                    const VecN<VXT>* yp[R];
 #pragma unroll
                     for (int a = 1; a <= R; a++) {
-                        const int mm = r - a, mp = r + a;  // rows relative to the first row
-                        ym[a - 1] = mm >= 0 ? q[mm < RYT ? mm : 0][(P + 4) % 9] : wv[-mm - 1];
-                        yp[a - 1] = mp < RYT ? q[mp][(P + 4) % 9] : wv[R + mp - RYT];
+                        const int mm = r - a, mp = r + a;
+                        ym[a - 1] = mm >= 0 ? &q[mm < TRY ? mm : 0][(P + 4) % 9] : &wv[-mm - 1];
+                        yp[a - 1] = mp < TRY ? &q[mp][(P + 4) % 9] : &wv[R + mp - TRY];
                     }
-                    float res[4];
+                    float res[VXT];
 #pragma unroll
-                    for (int c = 0; c < 4; c++) {
-                        const float cen = xw[4 + c];
-                        float v;
+                    for (int c = 0; c < VXT; c += 2) {
+                        const float2 cen = make_float2(xw[R + c], xw[R + c + 1]);
+                        float2 v;
                         if (MODE == 0) {
                             v = cen;
 #pragma unroll
                             for (int a = 1; a <= R; a++) {
-                                const float sx = __fadd_rn(xw[4 + c - a], xw[4 + c + a]);
-                                const float sy = __fadd_rn(f4(ym[a - 1], c), f4(yp[a - 1], c));
-                                const float sz = __fadd_rn(f4(q[r][(P + 4 - a) % 9], c), f4(q[r][(P + 4 + a) % 9], c));
-                                v = __fadd_rn(v, __fadd_rn(__fadd_rn(sx, sy), sz));
+                                const float2 sx = f2::add(make_float2(xw[R + c - a], xw[R + c + 1 - a]),
+                                                          make_float2(xw[R + c + a], xw[R + c + 1 + a]));
+                                const float2 sy = f2::add(make_float2(ym[a - 1]->v[c], ym[a - 1]->v[c + 1]),
+                                                          make_float2(yp[a - 1]->v[c], yp[a - 1]->v[c + 1]));
+                                const VecN<VXT>& zm = q[r][(P + 4 - a) % 9];
+                                const VecN<VXT>& zp = q[r][(P + 4 + a) % 9];
+                                const float2 sz = f2::add(make_float2(zm.v[c], zm.v[c + 1]), make_float2(zp.v[c], zp.v[c + 1]));
+                                v = f2::add(v, f2::add(f2::add(sx, sy), sz));
                             }
-                            v = __fmul_rn(v, coeff);
+                            v = f2::mul(v, f2::splat(coeff));
                         } else {
-                            v = wt.w[0] * cen;
+                            v = f2::mul(f2::splat(wt.w[0]), cen);
 #pragma unroll
-                            for (int a = 1; a <= R; a++)
-                                v += wt.w[a] * (((xw[4 + c - a] + xw[4 + c + a]) + (f4(ym[a - 1], c) + f4(yp[a - 1], c))) +
-                                                (f4(q[r][(P + 4 - a) % 9], c) + f4(q[r][(P + 4 + a) % 9], c)));
+                            for (int a = 1; a <= R; a++) {
+                                const float2 sx = f2::add(make_float2(xw[R + c - a], xw[R + c + 1 - a]),
+                                                          make_float2(xw[R + c + a], xw[R + c + 1 + a]));
+                                const float2 sy = f2::add(make_float2(ym[a - 1]->v[c], ym[a - 1]->v[c + 1]),
+                                                          make_float2(yp[a - 1]->v[c], yp[a - 1]->v[c + 1]));
+                                const VecN<VXT>& zm = q[r][(P + 4 - a) % 9];
+                                const VecN<VXT>& zp = q[r][(P + 4 + a) % 9];
+                                const float2 sz = f2::add(make_float2(zm.v[c], zm.v[c + 1]), make_float2(zp.v[c], zp.v[c + 1]));
+                                v = f2::fma(f2::splat(wt.w[a]), f2::add(f2::add(sx, sy), sz), v);
+                            }
                         }
-                        res[c] = v;
+                        res[c] = v.x;
+                        res[c + 1] = v.y;
                     }
                     const int yr = y + r;
                     if (!bad && x < nx + R && yr < ny + R) {
                         T* o = out + (size_t)k * plane + (size_t)yr * px + x;
-                        if (x + VX <= nx + R) {
-                            Vec4<T>::st(o, make_float4(res[0], res[1], res[2], res[3]));
+                        if (x + VXT <= nx + R) {
+                            stgv<T, VXT>(o, res);
                         } else {  // ragged last vector of a row: only the interior lanes
-                            for (int c = 0; c < VX && x + c < nx + R; c++) st<T>(o + c, res[c]);
+                            for (int c = 0; c < VXT && x + c < nx + R; c++) st<T>(o + c, res[c]);
                         }
                     }
                 }
@@ -450,7 +521,7 @@ __global__ void __launch_bounds__(16 * (VTY / RYT)) star_r4_tma(const __grid_con
     }
     if (bad && t == 0) {  // a wait gave up: report and let the copies still in flight land
         atomicOr(status, (unsigned)gb::ST_TMA_TIMEOUT);
-        for (int pl = max(pbase, last_issued - TNS + 1); pl <= last_issued; pl++) ready(pl);  // latest phase of each slot
+        for (int pl = max(pbase, last_issued - TNS + 1); pl <= last_issued; pl++) ready(pl, gb::tma::DRAIN_NS);
     }
 }
 
@@ -462,52 +533,63 @@ void launch_star(const T* in, T* out, int nx, int ny, int nz, int px, int kz, fl
     star_r4_sweep<T, MODE, RY><<<grd, blk, 0, st>>>(in, out, nx, ny, nz, px, ny + 2 * R, kz, coeff, w);
 }
 
+template <class T, int VXT>
+int run_star_tma(T** buf, int nx, int ny, int nz, int pitch, int iters, int mode, float coeff, StarW w, int kz, int* cur_index,
+                 cudaStream_t st)
+{
+    typedef TmaStar<T, VXT> Lay;
+    const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    CUtensorMap maps[2];
+    for (int n = 0; n < 2; n++)
+        GB_TRY(gb::tensor_map_3d(&maps[n], dt, sizeof(T), buf[n], nx + 2 * R, ny + 2 * R, nz + 2 * R, pitch, ny + 2 * R, Lay::SW,
+                                 Lay::SH));
+    unsigned* status;
+    GB_TRY(gb::status_word(&status));
+    constexpr int smem = Lay::smem();
+    auto kern = mode == 0 ? star_r4_tma<T, 0, VXT> : star_r4_tma<T, 1, VXT>;
+    GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    const int tkz = kz > 0 ? kz : 64;
+    dim3 blk(16, TTY / TRY), grd(gb::ceil_div(nx, Lay::TX), gb::ceil_div(ny, TTY), gb::ceil_div(nz, tkz));
+    int ci = 0;
+    for (int it = 0; it < iters; it++) {
+        kern<<<grd, blk, smem, st>>>(maps[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2 * R, tkz, coeff, w, status);
+        ci = 1 - ci;
+    }
+    GB_TRY(gb::launched("star_r4_tma"));
+    if (cur_index) *cur_index = ci;
+    return APPFIS_GB_OK;
+}
+
 template <class T>
-int run_star(T* a, T* b, int nx, int ny, int nz, int pitch, int iters, int mode, float coeff, const float* w5, int ry,
+int run_star(T* a, T* b, int nx, int ny, int nz, int pitch, int iters, int mode, float coeff, const float* w5, int tile,
              int kz, int* cur_index, cudaStream_t st)
 {
     StarW w = {{0, 0, 0, 0, 0}};
     if (w5)
         for (int n = 0; n < 5; n++) w.w[n] = w5[n];
     T* buf[2] = {a, b};
-    // TMA-staged tile when the rows are 16-byte aligned; else the register-staged vector tile when
-    // 4-element vectors are aligned; else the scalar tile
-    const bool tma = ry == 0 && (pitch * sizeof(T)) % 16 == 0 && gb::aligned16(a) && gb::aligned16(b);
-    const bool vec = ry == 0 && pitch % 4 == 0 && ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) %
-                                                    (sizeof(T) * 4)) == 0;
-    int ci = 0;
-    if (tma) {
-        const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
-        CUtensorMap maps[2];
-        for (int n = 0; n < 2; n++)
-            GB_TRY(gb::tensor_map_3d(&maps[n], dt, sizeof(T), buf[n], nx + 2 * R, ny + 2 * R, nz + 2 * R, pitch, ny + 2 * R, TSW,
-                                     TSH));
-        unsigned* status;
-        GB_TRY(gb::status_word(&status));
-        constexpr int smem = TmaStar<T>::smem();
-        auto kern = mode == 0 ? star_r4_tma<T, 0, TRY> : star_r4_tma<T, 1, TRY>;
-        GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        const int tkz = kz > 0 ? kz : 64;
-        dim3 blk(16, VTY / TRY), grd(gb::ceil_div(nx, VTX), gb::ceil_div(ny, VTY), gb::ceil_div(nz, tkz));
-        for (int it = 0; it < iters; it++) {
-            kern<<<grd, blk, smem, st>>>(maps[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2 * R, tkz, coeff, w, status);
-            ci = 1 - ci;
-        }
-        GB_TRY(gb::launched("star_r4_tma"));
-        if (cur_index) *cur_index = ci;
-        return APPFIS_GB_OK;
-    }
+    const bool rows16 = (pitch * sizeof(T)) % 16 == 0 && gb::aligned16(a) && gb::aligned16(b);
+    const bool vec4 = pitch % 4 == 0 && ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) % (sizeof(T) * 4)) == 0;
+    if (tile == APPFIS_GB_STAR_AUTO)  // TMA-staged when rows are 16-byte aligned, else vectors, else scalar
+        tile = rows16 ? APPFIS_GB_STAR_TMA_X4 : (vec4 ? APPFIS_GB_STAR_VEC : APPFIS_GB_STAR_SCALAR4);
+    if ((tile == APPFIS_GB_STAR_TMA_X4 || tile == APPFIS_GB_STAR_TMA_X2) && !rows16)
+        return gb::fail(APPFIS_GB_EINVAL, "star_r4: the TMA-staged tiles need 16-byte aligned rows and fields");
+    if (tile == APPFIS_GB_STAR_VEC && !vec4)
+        return gb::fail(APPFIS_GB_EINVAL, "star_r4: the vector tile needs a pitch of a multiple of 4 and aligned fields");
+    if (tile == APPFIS_GB_STAR_TMA_X4) return run_star_tma<T, 4>(buf, nx, ny, nz, pitch, iters, mode, coeff, w, kz, cur_index, st);
+    if (tile == APPFIS_GB_STAR_TMA_X2) return run_star_tma<T, 2>(buf, nx, ny, nz, pitch, iters, mode, coeff, w, kz, cur_index, st);
     if (kz <= 0) kz = 32;
+    int ci = 0;
     for (int it = 0; it < iters; it++) {
-        if (vec) {
+        if (tile == APPFIS_GB_STAR_VEC) {
             dim3 blk(16, 16), grd(gb::ceil_div(nx, VTX), gb::ceil_div(ny, VTY), gb::ceil_div(nz, kz));
             if (mode == 0) star_r4_vec<T, 0><<<grd, blk, 0, st>>>(buf[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2 * R, kz, coeff, w);
             else star_r4_vec<T, 1><<<grd, blk, 0, st>>>(buf[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2 * R, kz, coeff, w);
         } else if (mode == 0) {
-            if (ry == 2) launch_star<T, 0, 2>(buf[ci], buf[1 - ci], nx, ny, nz, pitch, kz, coeff, w, st);
+            if (tile == APPFIS_GB_STAR_SCALAR2) launch_star<T, 0, 2>(buf[ci], buf[1 - ci], nx, ny, nz, pitch, kz, coeff, w, st);
             else launch_star<T, 0, 4>(buf[ci], buf[1 - ci], nx, ny, nz, pitch, kz, coeff, w, st);
         } else {
-            if (ry == 2) launch_star<T, 1, 2>(buf[ci], buf[1 - ci], nx, ny, nz, pitch, kz, coeff, w, st);
+            if (tile == APPFIS_GB_STAR_SCALAR2) launch_star<T, 1, 2>(buf[ci], buf[1 - ci], nx, ny, nz, pitch, kz, coeff, w, st);
             else launch_star<T, 1, 4>(buf[ci], buf[1 - ci], nx, ny, nz, pitch, kz, coeff, w, st);
         }
         ci = 1 - ci;
@@ -522,21 +604,22 @@ int run_star(T* a, T* b, int nx, int ny, int nz, int pitch, int iters, int mode,
 extern "C" {
 
 int appfis_gb_star_r4(void* a, void* b, int dtype, int nx, int ny, int nz, int pitch, int iters, int mode, float coeff,
-                      const float* weights, int tile_rows, int zchunk, int* cur_index, void* stream)
+                      const float* weights, int tile, int zchunk, int* cur_index, void* stream)
 {
     if (!a || !b || a == b) return gb::fail(APPFIS_GB_EINVAL, "star_r4: null or aliased buffers");
     if (nx < 1 || ny < 1 || nz < 1 || pitch < nx + 2 * R) return gb::fail(APPFIS_GB_EINVAL, "star_r4: bad dims");
     if (mode != 0 && mode != 1) return gb::fail(APPFIS_GB_EINVAL, "star_r4: mode %d", mode);
     if (mode == 1 && !weights) return gb::fail(APPFIS_GB_EINVAL, "star_r4: weighted mode needs 5 weights");
     if (iters < 0) return gb::fail(APPFIS_GB_EINVAL, "star_r4: negative iteration count");
-    const int ry = tile_rows < 0 ? 0 : tile_rows;  // 0: vectorised tile when the rows are 16-byte aligned
-    if (ry != 0 && ry != 2 && ry != 4) return gb::fail(APPFIS_GB_EINVAL, "star_r4: tile_rows must be 0, 2 or 4");
-    const int kz = zchunk <= 0 ? 0 : zchunk;  // 0: the kernel's default (64 planes TMA-staged, 32 otherwise)
+    if (tile != APPFIS_GB_STAR_AUTO && tile != APPFIS_GB_STAR_SCALAR2 && tile != APPFIS_GB_STAR_SCALAR4 &&
+        tile != APPFIS_GB_STAR_TMA_X4 && tile != APPFIS_GB_STAR_TMA_X2 && tile != APPFIS_GB_STAR_VEC)
+        return gb::fail(APPFIS_GB_EINVAL, "star_r4: unknown tile %d", tile);
+    const int kz = zchunk <= 0 ? 0 : zchunk;  // 0: the tile's default (64 planes TMA-staged, 32 otherwise)
     cudaStream_t st = gb::as_stream(stream);
     if (dtype == APPFIS_GB_F32)
-        return run_star<float>((float*)a, (float*)b, nx, ny, nz, pitch, iters, mode, coeff, weights, ry, kz, cur_index, st);
+        return run_star<float>((float*)a, (float*)b, nx, ny, nz, pitch, iters, mode, coeff, weights, tile, kz, cur_index, st);
     if (dtype == APPFIS_GB_F16)
-        return run_star<__half>((__half*)a, (__half*)b, nx, ny, nz, pitch, iters, mode, coeff, weights, ry, kz, cur_index, st);
+        return run_star<__half>((__half*)a, (__half*)b, nx, ny, nz, pitch, iters, mode, coeff, weights, tile, kz, cur_index, st);
     return gb::fail(APPFIS_GB_EINVAL, "star_r4: dtype %d (F32 or F16)", dtype);
 }
 

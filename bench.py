@@ -584,6 +584,13 @@ def bench_fdtd(torch, gb, W, dev, sp, hbm):
     o16 = (ha if ci.value == 0 else hb).float()
     s32 = _time(torch, sp, run(a, b, f32, 0, 10), reps=1) / 10
     s16 = _time(torch, sp, run(ha, hb, h0, 3, 10), reps=1) / 10
+    # one step of each tile (APPFIS_GB_STAR_TMA_X4 / TMA_X2 / VEC), averaged over 10
+    tiles = {}
+    for tname, tid in (("tma_x4", 8), ("tma_x2", 9), ("vec", 10)):
+        for dname, x, y, dt in (("fp32", a, b, 0), ("fp16", ha, hb, 3)):
+            one = lambda: gb.call("appfis_gb_star_r4", x.data_ptr(), y.data_ptr(), dt, nx, ny, nz, nx + 8, 10, 1, 0.0, w, tid,
+                                  0, ctypes.byref(ci), sp.cuda_stream)
+            tiles["%s_%s_ms" % (tname, dname)] = _time(torch, sp, one, reps=1) / 10
     g32 = nx * ny * nz * 8 / (s32 * 1e-3) / 1e9
     g16 = nx * ny * nz * 4 / (s16 * 1e-3) / 1e9
     res["workload"] = "fdtd3d radius-4 star 512^3, 200 steps of u <- u + 0.1*L8(u), zero halo of 4"
@@ -593,6 +600,7 @@ def bench_fdtd(torch, gb, W, dev, sp, hbm):
     res["fp16_storage"] = {"glups": lups / (ms16 * 1e-3) / 1e9, "ms": ms16, "bytes_per_lup": 4, "sweep_ms": s16,
                            "kernel": "star_r4_tma<half>", "achieved_gbs": g16, "frac_of_hbm": g16 / hbm,
                            "traffic": profiled_traffic("star_r4_tma<half>"), "speedup_vs_plain": ms32 / ms16,
+                           "step_ms_by_tile": tiles,
                            "max_abs_diff_vs_fp32": float((o16 - o32).abs().max().item())}
     return res
 
@@ -701,7 +709,7 @@ def profile_case(name, local):
             (himeno_tma<1>, himeno_correct)
     fdtd:   512^3, 5 FP32 steps then 5 FP16 steps (star_r4_tma)
     heat:   1024^2, 16 iterations (2 heat2d_blocked launches)
-    flood:  4 domains of 512^2, 10 steps (one flood_persistent launch)"""
+    flood:  the 32-domain batch (80 M cells, ~2.6 GB), 20 steps (one flood_persistent launch)"""
     import torch
 
     import appfis_gb300 as gb
@@ -713,8 +721,10 @@ def profile_case(name, local):
         fn = {"himeno": bench_himeno, "fdtd": bench_fdtd, "heat": bench_heat}.get(name)
         if name == "flood":
             from appfis_gb300 import _lib
-            doms = [W.triton_domain(512, 512, 4242 + k) for k in range(4)]
-            _lib.flood_job(doms, 10.0, 0.5, 1e-3, 0.035, 600.0, 600.0, 1.0, max_steps=10, dtype=_lib.F32)
+            c = W.TRITON
+            doms = W.triton_batch(c["n_domains"], c["side_lo"], c["side_hi"], c["seed"])
+            _lib.flood_job(doms, c["dx"], c["courant"], c["hextra"], c["manning"], c["t_end"], c["t_end"], c["time_step"],
+                           max_steps=20, dtype=_lib.F32)
         else:
             profile_small(name, torch, gb, W, dev, sp)
         torch.cuda.synchronize(dev)

@@ -177,16 +177,24 @@ APPFIS_GB_API int appfis_gb_himeno_job(const float* coef_host, float* p_host, in
                                        float omega, int form, int period, double* gosa_host);
 
 /* ----------------------------------------------------------------------------- radius-4 star (FDTD3d) */
+#define APPFIS_GB_STAR_AUTO 0
+#define APPFIS_GB_STAR_SCALAR2 2 /* scalar tile, 2 rows per thread */
+#define APPFIS_GB_STAR_SCALAR4 4 /* scalar tile, 4 rows per thread */
+#define APPFIS_GB_STAR_TMA_X4 8  /* TMA-staged 64 x 16 tile, 4 x points x 2 rows per thread */
+#define APPFIS_GB_STAR_TMA_X2 9  /* TMA-staged 32 x 16 tile, 2 x points x 2 rows per thread */
+#define APPFIS_GB_STAR_VEC 10    /* register-staged 64 x 16 tile of 4-element vectors */
 /* Replaces the per-step Execute3D(config, coeff, radius, cur, next) of the FDTD3d functor
  * (FDTD3d/src/fdtd3d_appfis.hpp:84-87,129-143) with radius 4 on a DUAL grid with a ghost halo of
  * width 4 (a, b: padded (nx+8) x (ny+8) x (nz+8), pitch >= nx+8, halo held at its values).
  * mode 0: the reference form  v = c + sum_{a=1..4} ((x-a + x+a) + (y-a + y+a) + (z-a + z+a)),
  *         v *= coeff  (same order; FP32 results bit-identical to the reference CPU path).
  * mode 1: weighted form  v = w[0]*c + sum_a w[a]*((x-a + x+a) + (y-a + y+a) + (z-a + z+a)).
- * dtype: APPFIS_GB_F32 or APPFIS_GB_F16 (storage).  tile_rows (2 or 4, 0 = 4) and zchunk (planes
- * per CTA, 0 = 64) select the tile shape (see appfis_gb_star_r4_tune). */
+ * dtype: APPFIS_GB_F32 or APPFIS_GB_F16 (storage).  tile selects the kernel (APPFIS_GB_STAR_*;
+ * AUTO: the TMA-staged tile when rows and fields are 16-byte aligned, else the vector tile when
+ * 4-element vectors are aligned, else the scalar tile; all give the same results).  zchunk: z
+ * planes per CTA (0 = the tile's default: 64 TMA-staged, 32 otherwise). */
 APPFIS_GB_API int appfis_gb_star_r4(void* a, void* b, int dtype, int nx, int ny, int nz, int pitch, int iters, int mode,
-                                    float coeff, const float* weights, int tile_rows, int zchunk, int* cur_index,
+                                    float coeff, const float* weights, int tile, int zchunk, int* cur_index,
                                     void* stream);
 
 /* ----------------------------------------------------------------------------- Triton flood model */

@@ -52,6 +52,33 @@ def test_reference_form_vs_oracle(gb, torch_cuda, nx, ny, nz, iters, ry, kz, pit
     assert np.array_equal(out, O.star_r4(f, iters, coeff=0.1))
 
 
+TMA_X4, TMA_X2, VEC = 8, 9, 10  # APPFIS_GB_STAR_* tiles
+
+
+@pytest.mark.parametrize("tile", [TMA_X4, TMA_X2, VEC])
+@pytest.mark.parametrize("nx,ny,nz,iters,kz,pitch", [(64, 70, 33, 2, 16, 72), (37, 29, 11, 3, 0, 48), (3, 17, 9, 2, 4, 12),
+                                                     (95, 9, 20, 2, 0, 104)])
+def test_every_tile_reference_form(gb, torch_cuda, tile, nx, ny, nz, iters, kz, pitch):
+    f = W.fdtd_padded(nx, ny, nz, 3 * nx + nz)
+    out = run(gb, torch_cuda, f, iters, 0, 0.1, pitch=pitch, ry=tile, kz=kz)
+    assert np.array_equal(out, O.star_r4(f, iters, coeff=0.1))
+
+
+@pytest.mark.parametrize("tile", [TMA_X4, TMA_X2])
+def test_tma_tiles_fp16_weighted(gb, torch_cuda, tile):
+    w = W.fdtd_weights()
+    f = W.fdtd_padded(70, 33, 21, 17)
+    a = run(gb, torch_cuda, f, 5, 1, weights=w, dtype="f16", pitch=80, ry=tile)
+    ref64 = O.star_r4(f.astype(np.float64), 5, weights=w, dtype=np.float64)
+    assert np.abs(a - ref64).max() < 2e-3
+
+
+def test_tile_needs_aligned_rows(gb, torch_cuda):
+    f = W.fdtd_padded(9, 5, 3, 1)
+    with pytest.raises(RuntimeError):
+        run(gb, torch_cuda, f, 1, 0, 0.1, pitch=18, ry=TMA_X2)  # 72-byte rows
+
+
 def test_weighted_form_vs_oracle(gb, torch_cuda):
     w = W.fdtd_weights()
     f = W.fdtd_padded(48, 40, 36, 5)
