@@ -102,88 +102,147 @@ __device__ __forceinline__ bool is_active(const Ctl* ctl, int cur, int d, const 
 }
 
 // ---------------------------------------------------------------- phase A: fix + dt
+// The domain descriptor arrives by value (registers): read through the shared-memory copy, every
+// field would be reloaded after each global store, which the compiler cannot prove disjoint.
+// Rows are processed in groups of FA_ROWS with their h, qx, qy loads issued together, so a
+// warp has several rows of loads in flight instead of one.
+constexpr int FA_ROWS = 4;
+
 template <class T>
-__device__ void phase_a(const Dom<T>& D, Ctl* ctl, int cur, int d, long long local, bool fix, bool want_dt, const Params& p)
+__device__ void phase_a(const Dom<T> D, Ctl* ctl, int cur, int d, long long local, int b, bool fix, bool want_dt,
+                        const Params& p)
 {
     const int lane = threadIdx.x & 31;
     const int sx = (int)(local % D.strips_x), sy = (int)(local / D.strips_x);
     const int i = 1 + sx * 32 + lane;
     const int j0 = 1 + sy * ROWS, j1 = min(j0 + ROWS, D.ny + 1);
-    const int b = ctl->steps[cur][d] & 1;
-    const T* h = D.h[b];
-    T* qx = D.qx[b];
-    T* qy = D.qy[b];
+    const T* __restrict__ h = D.h[b];
+    T* __restrict__ qx = D.qx[b];
+    T* __restrict__ qy = D.qy[b];
+    const T* __restrict__ dem = D.dem;
+    const int px = D.px;
     const T hextra = (T)p.hextra, E = K<T>::dry(), G = K<T>::g();
     const T dx = (T)p.dx, cn = (T)p.cn;
-    double mn = (double)K<T>::big();
+    T mn = K<T>::big();  // min in T (exact), widened once per warp: no per-cell FP64 work in float
     if (i <= D.nx) {
-        for (int j = j0; j < j1; j++) {
-            const size_t c = (size_t)j * D.px + i;
-            const T hij = h[c];
-            T qxv = qx[c], qyv = qy[c];
-            if (fix && hij > hextra) {  // triton_appfis.hpp:1095-1112
-                const T zij = D.dem[c];
-                const T lvl = hij + zij;
-                if (((lvl < D.dem[c + 1]) && (h[c + 1] < E)) || ((lvl < D.dem[c - 1]) && (h[c - 1] < E))) {
-                    qxv = T(0);
-                    qx[c] = qxv;
-                }
-                if (((lvl < D.dem[c - D.px]) && (h[c - D.px] < E)) || ((lvl < D.dem[c + D.px]) && (h[c + D.px] < E))) {
-                    qyv = T(0);
-                    qy[c] = qyv;
-                }
+        for (int jb = j0; jb < j1; jb += FA_ROWS) {
+            T hv[FA_ROWS], qxv[FA_ROWS], qyv[FA_ROWS];
+#pragma unroll
+            for (int r = 0; r < FA_ROWS; r++) {
+                const size_t c = (size_t)(jb + r) * px + i;
+                const bool in = jb + r < j1;
+                hv[r] = in ? h[c] : T(0);
+                qxv[r] = in ? qx[c] : T(0);
+                qyv[r] = in ? qy[c] : T(0);
             }
-            if (want_dt && hij > hextra) {  // triton_appfis.hpp:567-586
-                const T dtx = dx / (fabs(qxv / hij) + sqrt(G * hij));
-                const T dty = dx / (fabs(qyv / hij) + sqrt(G * hij));
-                const T v = dtx < dty ? cn * dtx : cn * dty;
-                mn = fmin(mn, (double)v);
+#pragma unroll
+            for (int r = 0; r < FA_ROWS; r++) {
+                const size_t c = (size_t)(jb + r) * px + i;
+                const T hij = hv[r];
+                if (!(hij > hextra)) continue;  // dry: no fix, no dt (rows past j1 hold 0)
+                T qxr = qxv[r], qyr = qyv[r];
+                if (fix) {  // triton_appfis.hpp:1095-1112
+                    const T lvl = hij + dem[c];
+                    if (((lvl < dem[c + 1]) && (h[c + 1] < E)) || ((lvl < dem[c - 1]) && (h[c - 1] < E))) {
+                        qxr = T(0);
+                        qx[c] = qxr;
+                    }
+                    if (((lvl < dem[c - px]) && (h[c - px] < E)) || ((lvl < dem[c + px]) && (h[c + px] < E))) {
+                        qyr = T(0);
+                        qy[c] = qyr;
+                    }
+                }
+                if (want_dt) {  // triton_appfis.hpp:567-586
+                    const T dtx = dx / (fabs(qxr / hij) + sqrt(G * hij));
+                    const T dty = dx / (fabs(qyr / hij) + sqrt(G * hij));
+                    const T v = dtx < dty ? cn * dtx : cn * dty;
+                    mn = v < mn ? v : mn;
+                }
             }
         }
     }
     if (want_dt) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mn = fmin(mn, __shfl_down_sync(0xffffffffu, mn, o));
-        if (lane == 0 && mn < (double)K<T>::big())
-            atomicMin(&ctl->dtbits[cur][d], (unsigned long long)__double_as_longlong(mn));
+        for (int o = 16; o > 0; o >>= 1) {
+            const T other = __shfl_down_sync(0xffffffffu, mn, o);
+            mn = other < mn ? other : mn;
+        }
+        if (lane == 0 && mn < K<T>::big())
+            atomicMin(&ctl->dtbits[cur][d], (unsigned long long)__double_as_longlong((double)mn));
     }
 }
 
 // ---------------------------------------------------------------- phase B: fluxes + update
+// A cell's raw state (h, qx, qy, z); zero outside the padded row.
 template <class T>
-__device__ __forceinline__ Cell<T> load_cell(const Dom<T>& D, int b, int i, int j)
+struct Raw {
+    T h, qx, qy, z;
+};
+
+template <class T>
+__device__ __forceinline__ Raw<T> load_raw(const T* __restrict__ h, const T* __restrict__ qx, const T* __restrict__ qy,
+                                           const T* __restrict__ dem, int px, int nx, int i, int j)
 {
-    if (i > D.nx + 1) return make_cell<T>(T(0), T(0), T(0), T(0));
-    const size_t c = (size_t)j * D.px + i;
-    return make_cell<T>(D.h[b][c], D.qx[b][c], D.qy[b][c], D.dem[c]);
+    if (i > nx + 1) return Raw<T>{T(0), T(0), T(0), T(0)};
+    const size_t c = (size_t)j * px + i;
+    return Raw<T>{h[c], qx[c], qy[c], dem[c]};
 }
 
 template <class T>
-__device__ void phase_b(const Dom<T>& D, Ctl* ctl, int cur, int d, long long local, const Params& p)
+__device__ __forceinline__ Cell<T> cell_of(const Raw<T>& r)
+{
+    return make_cell<T>(r.h, r.qx, r.qy, r.z);
+}
+
+// Each warp marches its strip's rows; the loads of row j+2 (and the lane-0 / lane-31 neighbour
+// cells of row j+1) are issued while row j is computed.
+template <class T>
+__device__ void phase_b(const Dom<T> D, long long local, int b, T dt, const Params& p)
 {
     const int lane = threadIdx.x & 31;
     const int sx = (int)(local % D.strips_x), sy = (int)(local / D.strips_x);
     const int i = 1 + sx * 32 + lane;
     const int j0 = 1 + sy * ROWS, j1 = min(j0 + ROWS, D.ny + 1);
     const bool act = i <= D.nx;
-    const int b = ctl->steps[cur][d] & 1;
-    const T dt = (T)step_dt(ctl, cur, d, p, (double)K<T>::big());
     const T dx = (T)p.dx, hextra = (T)p.hextra;
     const T one = T(1), zero = T(0);
+    const T* __restrict__ h = D.h[b];
+    const T* __restrict__ qx = D.qx[b];
+    const T* __restrict__ qy = D.qy[b];
+    const T* __restrict__ dem = D.dem;
+    const T* __restrict__ n2 = D.n2;
+    T* __restrict__ ho_ = D.h[1 - b];
+    T* __restrict__ qxo_ = D.qx[1 - b];
+    T* __restrict__ qyo_ = D.qy[1 - b];
+    const int px = D.px, nx = D.nx, ny = D.ny;
+    const Raw<T> zr = {zero, zero, zero, zero};
 
-    Cell<T> cj = load_cell(D, b, i, j0);
+    Cell<T> cj = cell_of(load_raw(h, qx, qy, dem, px, nx, i, j0));
+    Raw<T> rn = load_raw(h, qx, qy, dem, px, nx, i, j0 + 1);  // rows j0+1 <= ny+1 always exist
+    Raw<T> side = zr;                                           // lane 31: cell i+1, lane 0: cell i-1 of row j
+    if (lane == 31) side = load_raw(h, qx, qy, dem, px, nx, i + 1, j0);
+    if (lane == 0) side = load_raw(h, qx, qy, dem, px, nx, i - 1, j0);
     T ycar[3] = {zero, zero, zero};  // rhs0 Y part of row j (from face j|j-1)
     bool ywet = false;
     if (act) {
-        const Cell<T> cm = load_cell(D, b, i, j0 - 1);
+        const Cell<T> cm = cell_of(load_raw(h, qx, qy, dem, px, nx, i, j0 - 1));
         T r2[3];
         ywet = face<T>(cj, cm, zero, one, dx, dt, hextra, ycar, r2);
     }
     for (int j = j0; j < j1; j++) {
-        const Cell<T> cn_ = load_cell(D, b, i, j + 1);
+        // prefetch: row j+2, the side cell of row j+1, this cell's n^2
+        const Raw<T> rnn = j + 2 <= ny + 1 ? load_raw(h, qx, qy, dem, px, nx, i, j + 2) : zr;
+        Raw<T> sidn = zr;
+        if (j + 1 < j1) {
+            if (lane == 31) sidn = load_raw(h, qx, qy, dem, px, nx, i + 1, j + 1);
+            if (lane == 0) sidn = load_raw(h, qx, qy, dem, px, nx, i - 1, j + 1);
+        }
+        const size_t c = (size_t)j * px + i;
+        const T n2v = act ? n2[c] : zero;
+        const Cell<T> cn_ = cell_of(rn);
         // X face i|i+1 of row j
         Cell<T> right = shfl_cell(cj, 1, true);
-        if (lane == 31 && act) right = load_cell(D, b, i + 1, j);
+        if (lane == 31 && act) right = cell_of(side);
         T xr1[3] = {zero, zero, zero}, xr2[3] = {zero, zero, zero};
         bool xwet = false;
         if (act) xwet = face<T>(cj, right, one, zero, dx, dt, hextra, xr1, xr2);
@@ -195,9 +254,8 @@ __device__ void phase_b(const Dom<T>& D, Ctl* ctl, int cur, int d, long long loc
         lr[2] = __shfl_up_sync(0xffffffffu, xr2[2], 1);
         lwet = __shfl_up_sync(0xffffffffu, (int)xwet, 1) != 0;
         if (lane == 0 && act) {
-            const Cell<T> left = load_cell(D, b, i - 1, j);
             T t1[3];
-            lwet = face<T>(left, cj, one, zero, dx, dt, hextra, t1, lr);
+            lwet = face<T>(cell_of(side), cj, one, zero, dx, dt, hextra, t1, lr);
         }
         // Y face j+1|j: id1 = row j+1, id2 = row j
         T yn1[3] = {zero, zero, zero}, yr2[3] = {zero, zero, zero};
@@ -212,25 +270,41 @@ __device__ void phase_b(const Dom<T>& D, Ctl* ctl, int cur, int d, long long loc
                 r1[k] = lwet ? lr[k] : zero;
                 if (ynwet) r1[k] = r1[k] + yr2[k];
             }
-            const size_t c = (size_t)j * D.px + i;
-            T ho, qxo, qyo;
-            update<T>(cj.h, cj.qx, cj.qy, D.n2[c], r0, r1, dt, hextra, ho, qxo, qyo);
-            D.h[1 - b][c] = ho;
-            D.qx[1 - b][c] = qxo;
-            D.qy[1 - b][c] = qyo;
+            T hn, qxn, qyn;
+            update<T>(cj.h, cj.qx, cj.qy, n2v, r0, r1, dt, hextra, hn, qxn, qyn);
+            ho_[c] = hn;
+            qxo_[c] = qxn;
+            qyo_[c] = qyn;
         }
 #pragma unroll
         for (int k = 0; k < 3; k++) ycar[k] = yn1[k];
         ywet = ynwet;
         cj = cn_;
+        rn = rnn;
+        side = sidn;
     }
 }
 
+// Per-domain control of a phase (state buffer, fix / dt / step flags, the step's dt), evaluated
+// once per CTA per phase by one thread per domain into shared memory: the strip loops then do
+// no FP64 work (this part's FP64 rate is a small fraction of its FP32 rate).
 template <class T>
-__global__ void __launch_bounds__(256) flood_persistent(const Dom<T>* __restrict__ gdoms, Ctl* ctl, Params p)
+struct DomCtl {
+    T dt[MAXD];
+    unsigned char flags[MAXD];  // bit 0: state buffer b, bit 1: fix, bit 2: wants dt / runs phase B
+};
+
+// CTAs per SM the FP32 kernel's register allocation targets (FP64: 1).
+#ifndef FLOOD_F32_MIN_BLOCKS
+#define FLOOD_F32_MIN_BLOCKS 3
+#endif
+
+template <class T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1) flood_persistent(const Dom<T>* __restrict__ gdoms, Ctl* ctl,
+                                                                                Params p)
 {
     __shared__ Dom<T> doms[MAXD];
-    __shared__ int s_any;
+    __shared__ DomCtl<T> dc;
     for (int k = threadIdx.x; k < p.ndom; k += blockDim.x) doms[k] = gdoms[k];
     __syncthreads();
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -240,20 +314,29 @@ __global__ void __launch_bounds__(256) flood_persistent(const Dom<T>* __restrict
     for (int n = 0;; n++) {
         const int cur = n & 1;
         // phase A
-        for (long long s = warp; s < p.total_strips; s += nwarps) {
-            const int d = find_domain(doms, p.ndom, s);
+        if (threadIdx.x < p.ndom) {
+            const int d = threadIdx.x;
             const bool fix = ctl->steps[cur][d] != ctl->steps[1 - cur][d];
             const bool want = is_active(ctl, cur, d, p);
-            if (fix || want) phase_a<T>(doms[d], ctl, cur, d, s - doms[d].strip0, fix, want, p);
-        }
-        if (!grid_barrier(ctl)) return;
-        if (threadIdx.x == 0) {
-            int any = 0;
-            for (int d = 0; d < p.ndom; d++) any |= is_active(ctl, cur, d, p) ? 1 : 0;
-            s_any = any;
+            dc.flags[d] = (unsigned char)((ctl->steps[cur][d] & 1) | (fix ? 2 : 0) | (want ? 4 : 0));
         }
         __syncthreads();
-        if (!s_any) {
+        for (long long s = warp; s < p.total_strips; s += nwarps) {
+            const int d = find_domain(doms, p.ndom, s);
+            const int f = dc.flags[d];
+            if (f & 6) phase_a<T>(doms[d], ctl, cur, d, s - doms[d].strip0, f & 1, (f & 2) != 0, (f & 4) != 0, p);
+        }
+        if (!grid_barrier(ctl)) return;
+        int active = 0;
+        if (threadIdx.x < p.ndom) {
+            const int d = threadIdx.x;
+            active = is_active(ctl, cur, d, p) ? 1 : 0;
+            const double dt = active ? step_dt(ctl, cur, d, p, big) : 0.0;
+            const bool run = active && dt > 1e-9 * p.time_step;
+            dc.dt[d] = (T)dt;
+            dc.flags[d] = (unsigned char)((ctl->steps[cur][d] & 1) | (run ? 4 : 0));
+        }
+        if (!__syncthreads_or(active)) {
             if (blockIdx.x == 0 && threadIdx.x == 0)  // leave the final scalars in both halves
                 for (int d = 0; d < p.ndom; d++) {
                     ctl->simtime[1 - cur][d] = ctl->simtime[cur][d];
@@ -265,8 +348,8 @@ __global__ void __launch_bounds__(256) flood_persistent(const Dom<T>* __restrict
         // phase B
         for (long long s = warp; s < p.total_strips; s += nwarps) {
             const int d = find_domain(doms, p.ndom, s);
-            if (is_active(ctl, cur, d, p) && step_dt(ctl, cur, d, p, big) > 1e-9 * p.time_step)
-                phase_b<T>(doms[d], ctl, cur, d, s - doms[d].strip0, p);
+            const int f = dc.flags[d];
+            if (f & 4) phase_b<T>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p);
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) {  // commit the per-domain scalars of step n
             for (int d = 0; d < p.ndom; d++) {

@@ -36,18 +36,6 @@ __device__ __forceinline__ uint32_t rule_bytes(uint32_t cnt, uint32_t c, uint32_
     }
 }
 
-// Per bit lane (bits form): cnt as bit slices r0..r3.
-template <int RULE>
-__device__ __forceinline__ uint32_t rule_bits(uint32_t r0, uint32_t r1, uint32_t r2, uint32_t r3, uint32_t c, uint32_t o)
-{
-    if (RULE == APPFIS_GB_LIFE_REFERENCE) {
-        uint32_t birth = r0 & r1 & ~(r2 | r3);
-        uint32_t keep = ~r3 & ((~r2 & r1) | (r2 & ~r1 & ~r0));
-        return (c & keep & o) | (~c & (birth | o));
-    } else {
-        return r1 & ~(r2 | r3) & (r0 | c);
-    }
-}
 
 // ------------------------------------------------------------------------------ generic form
 // One thread per cell, any nx, ny (used when nx is not a multiple of 16).
@@ -165,8 +153,35 @@ __global__ void __launch_bounds__(256) life_u8_swar(const uint8_t* __restrict__ 
 struct RowBits {
     uint32_t w;       // 32 cells
     uint32_t a0, a1;  // left + self + right as 2-bit slices
-    uint32_t h0, h1;  // left + right as 2-bit slices
 };
+
+// New word from the row sums of the rows above, at and below (each left + self + right, 0..3).
+// S = up + mid + dn is the 3x3 sum including the cell, so the neighbour count is S - c:
+//   reference rule (S234 with the stale carry): a live cell keeps o when S is 3, 4 or 5 and dies
+//     otherwise; a dead cell is born when S is 3 and otherwise keeps o;
+//   B3/S23: a live cell survives when S is 3 or 4; a dead cell is born when S is 3.
+// Only S mod 8 is formed (S0..S2): S = 8 and 9 read as 0 and 1, which neither rule distinguishes
+// from the true values (no birth, no survival either way).  Two full adders with 3-input logic
+// and one half adder: 7 operations for the count, 4 for the rule.
+template <int RULE>
+__device__ __forceinline__ uint32_t life_combine(const RowBits& up, const RowBits& mid, const RowBits& dn, uint32_t o)
+{
+    const uint32_t s0 = up.a0 ^ mid.a0 ^ dn.a0;
+    const uint32_t c1 = (up.a0 & mid.a0) | (up.a0 & dn.a0) | (mid.a0 & dn.a0);
+    const uint32_t x = up.a1 ^ mid.a1 ^ dn.a1;
+    const uint32_t y = (up.a1 & mid.a1) | (up.a1 & dn.a1) | (mid.a1 & dn.a1);
+    const uint32_t s1 = x ^ c1, z = x & c1;
+    const uint32_t s2 = y ^ z;
+    const uint32_t eq3 = ~s2 & s1 & s0;
+    const uint32_t c = mid.w;
+    if (RULE == APPFIS_GB_LIFE_REFERENCE) {
+        const uint32_t in345 = eq3 | (s2 & ~s1);
+        return (c & in345 & o) | (~c & (eq3 | o));
+    } else {
+        const uint32_t in34 = eq3 | (s2 & ~s1 & ~s0);
+        return (c & in34) | (~c & eq3);
+    }
+}
 struct RawBits {
     uint32_t w, lw, rw;
 };
@@ -195,8 +210,6 @@ __device__ __forceinline__ RowBits finish_row_bits(const RawBits& raw, int xw, i
     r.w = w;
     r.a0 = L ^ w ^ R;
     r.a1 = (L & w) | (R & (L ^ w));
-    r.h0 = L ^ R;
-    r.h1 = L & R;
     return r;
 }
 
@@ -225,15 +238,7 @@ __global__ void __launch_bounds__(256) life_bits_sweep(const uint32_t* __restric
                 if (RULE == APPFIS_GB_LIFE_REFERENCE && active) onext = out[(size_t)(j + 1) * nw + xw];
             }
             const RowBits dn = finish_row_bits(rdn, xw, nw, lane);
-            if (active) {
-                // count = up(3-input) + mid(2-input) + dn(3-input), bit-sliced
-                const uint32_t t0 = up.a0 ^ mid.h0, c0 = up.a0 & mid.h0;
-                const uint32_t t1 = up.a1 ^ mid.h1 ^ c0, t2 = (up.a1 & mid.h1) | (c0 & (up.a1 ^ mid.h1));
-                const uint32_t r0 = t0 ^ dn.a0, k0 = t0 & dn.a0;
-                const uint32_t r1 = t1 ^ dn.a1 ^ k0, k1 = (t1 & dn.a1) | (k0 & (t1 ^ dn.a1));
-                const uint32_t r2 = t2 ^ k1, r3 = t2 & k1;
-                out[(size_t)j * nw + xw] = rule_bits<RULE>(r0, r1, r2, r3, mid.w, o);
-            }
+            if (active) out[(size_t)j * nw + xw] = life_combine<RULE>(up, mid, dn, o);
             up = mid;
             mid = dn;
             rdn = rnext;
@@ -261,9 +266,8 @@ constexpr int TB_RR = TB_ROWS + 2 * TB_STEPS;
 // Row summary of one word for the bit-sliced neighbour count.  Lanes 0 / 31 get their own word
 // back from the shuffles, so their outer bit is wrong; those lanes are the stale halo, whose
 // wrong bits travel one cell per generation and never reach an output word.
-__device__ __forceinline__ RowBits tile_row(uint32_t w, int lane)
+__device__ __forceinline__ RowBits tile_row(uint32_t w)
 {
-    (void)lane;
     const uint32_t lw = __shfl_up_sync(FULL, w, 1);
     const uint32_t rw = __shfl_down_sync(FULL, w, 1);
     const uint32_t L = __funnelshift_l(lw, w, 1), R = __funnelshift_r(w, rw, 1);
@@ -271,29 +275,7 @@ __device__ __forceinline__ RowBits tile_row(uint32_t w, int lane)
     r.w = w;
     r.a0 = L ^ w ^ R;
     r.a1 = (L & w) | (R & (L ^ w));
-    r.h0 = L ^ R;
-    r.h1 = L & R;
     return r;
-}
-
-// Count bits r0..r2 of up + mid + dn (the count-8 bit is not formed: with it dropped a count of
-// 8 reads as 0, and both rules treat 0 and 8 alike — no birth, no survival).
-template <int RULE>
-__device__ __forceinline__ uint32_t life_combine(const RowBits& up, const RowBits& mid, const RowBits& dn, uint32_t o)
-{
-    const uint32_t t0 = up.a0 ^ mid.h0, c0 = up.a0 & mid.h0;
-    const uint32_t t1 = up.a1 ^ mid.h1 ^ c0, t2 = (up.a1 & mid.h1) | (c0 & (up.a1 ^ mid.h1));
-    const uint32_t r0 = t0 ^ dn.a0, k0 = t0 & dn.a0;
-    const uint32_t r1 = t1 ^ dn.a1 ^ k0, k1 = (t1 & dn.a1) | (k0 & (t1 ^ dn.a1));
-    const uint32_t r2 = t2 ^ k1;
-    const uint32_t c = mid.w;
-    if (RULE == APPFIS_GB_LIFE_REFERENCE) {
-        const uint32_t birth = r0 & r1 & ~r2;                      // count 3
-        const uint32_t keep = (~r2 & r1) | (r2 & ~r1 & ~r0);       // count 2, 3, 4
-        return (c & keep & o) | (~c & (birth | o));
-    } else {
-        return r1 & ~r2 & (r0 | c);                                // count 3, or count 2 and alive
-    }
 }
 
 template <int RULE>
@@ -325,10 +307,10 @@ __global__ void __launch_bounds__(TB_WARPS * 32) life_bits_tb(const uint32_t* __
             const int lo = t, n = TB_RR - 2 * t, chunk = (n + TB_WARPS - 1) / TB_WARPS;
             const int r0 = lo + warp * chunk, r1 = min(lo + n, r0 + chunk);
             if (r0 < r1) {
-                RowBits up = tile_row(cur[r0 - 1][lane], lane);
-                RowBits mid = tile_row(cur[r0][lane], lane);
+                RowBits up = tile_row(cur[r0 - 1][lane]);
+                RowBits mid = tile_row(cur[r0][lane]);
                 for (int r = r0; r < r1; r++) {
-                    const RowBits dn = tile_row(cur[r + 1][lane], lane);
+                    const RowBits dn = tile_row(cur[r + 1][lane]);
                     const uint32_t o = RULE == APPFIS_GB_LIFE_REFERENCE ? old[r][lane] : 0u;
                     old[r][lane] = life_combine<RULE>(up, mid, dn, o);
                     up = mid;
