@@ -5,10 +5,11 @@
 // on a DUAL p grid and 12 SINGLE coefficient grids (:74-86, :108-114).  The reference computes
 // no gosa; ss is exactly its :195 expression.
 //
-// Plain form: one launch per sweep (himeno_ring<0>, below): 2.5-D z-march with the p planes in
-// a shared ring; the 12 coefficient streams are read once, one plane ahead.  The sum uses
-// round-to-nearest intrinsics in the reference's order (no FMA contraction), so p is
-// bit-identical to the reference CPU path.
+// Plain form: one launch per sweep, a 2.5-D z-march with the p planes in a shared ring and the
+// 12 coefficient streams read once: himeno_tma (tiles moved by the tensor memory accelerator)
+// when rows and fields are 16-byte aligned, else himeno_ring<0> (register-prefetched loads).
+// The sum uses round-to-nearest intrinsics in the reference's order (no FMA contraction), so p
+// is bit-identical to the reference CPU path.
 //
 // Defect-correction form (FP16 storage, FP32 arithmetic).  With p = P + e (P an FP32 master
 // frozen between corrections) the Jacobi update p' = p + w*bnd*(a3*(N p + wrk1) - p) becomes
@@ -19,7 +20,8 @@
 // every point coherently): 30 B per point per sweep instead of 56.  Every `period` sweeps a
 // correction pass folds e into P, recomputes D from the FP32 coefficients and restarts e at 0,
 // which bounds the FP16 error to the last period's correction.  The sweep's own ss is
-// (e' - e)/w (FP32, before rounding e').
+// (e' - e)/w (FP32, before rounding e').  Inner sweeps: himeno_mixed2 (TMA-staged, two points
+// per thread) when the FP16 rows are 16-byte aligned, else himeno_ring<1>.
 #include <cuda_fp16.h>
 
 #include <type_traits>
@@ -309,39 +311,36 @@ __global__ void __launch_bounds__(RX* RY) himeno_ring(Coef12 cf, H10 hf, const v
     if (gosa) gosa_reduce(g.value(), partials, ticket, gosa);
 }
 
-// ---------------------------------------------------------------- TMA-staged 2.5-D forms
-// Same tile, z-march and arithmetic as himeno_ring, but every stream is moved by the tensor
-// memory accelerator: for plane k, one pipeline stage holds the twelve per-point tiles of plane
-// k (32 x 8 each) and the iterated field's plane k+1 (40 x 10 FP32 or 48 x 10 FP16, the halo
-// included, its x origin rounded down to a 16-byte boundary).  Thread 0 keeps S stages in
-// flight; the other threads only read shared memory.  The CTA's x tile starts on a 32-point
-// boundary of the padded row (thread tx owns padded x = 32*bx + tx, interior points only), so
-// every tile copy starts 16-byte aligned; this needs a pitch of a multiple of 4 (FP32) or 8
-// (FP16) elements and 16-byte aligned fields.
+// ---------------------------------------------------------------- TMA-staged FP32 sweep
+// Same tile, z-march and arithmetic as himeno_ring<0>, but every stream is moved by the tensor
+// memory accelerator: for plane k, one pipeline stage holds the twelve coefficient tiles of
+// plane k (32 x 8 each) and p's plane k+1 (40 x 10, the halo included, its x origin rounded down
+// to a 16-byte boundary).  Thread 0 keeps S stages in flight; the other threads only read
+// shared memory.  The CTA's x tile starts on a 32-point boundary of the padded row (thread tx
+// owns padded x = 32*bx + tx, interior points only), so every tile copy starts 16-byte aligned;
+// this needs a pitch of a multiple of 4 elements and 16-byte aligned fields.
 struct TileMaps {
-    CUtensorMap m[13];  // 0..11: the per-point fields (see himeno_tma), 12: the iterated field
+    CUtensorMap m[13];  // 0..11: the per-point fields, 12: the iterated field
 };
 
-template <int MODE>
 struct TmaLayout {
-    typedef typename std::conditional<MODE == 0, float, __half>::type L;
-    static constexpr int XO = MODE == 0 ? 4 : 8;          // ring box x origin = tile x - XO
-    static constexpr int W = RX + 2 * XO;                 // ring box width (40 / 48)
-    static constexpr int RB = W * (RY + 2) * (int)sizeof(L);  // ring box bytes
+    static constexpr int XO = 4;                          // ring box x origin = tile x - XO
+    static constexpr int W = RX + 2 * XO;                 // ring box width (40)
+    static constexpr int RB = W * (RY + 2) * 4;           // ring box bytes
     static constexpr int PB = (RB + 127) / 128 * 128;     // ring slot bytes
-    static constexpr int CT = MODE == 0 ? 12 * 1024 : 10 * 512 + 1024 + 512;  // per-point tiles of one plane
-    __host__ __device__ static constexpr int tile_off(int n) { return MODE == 0 ? n * 1024 : (n < 10 ? n * 512 : (n == 10 ? 5120 : 6144)); }
+    static constexpr int CT = 12 * 1024;                  // the coefficient tiles of one plane
+    __host__ __device__ static constexpr int tile_off(int n) { return n * 1024; }
     static constexpr int smem(int S) { return S * CT + (S + 2) * PB + S * 8; }
 };
 
-template <int MODE, int S>
-__global__ void __launch_bounds__(RX* RY) himeno_tma(const __grid_constant__ TileMaps maps, void* __restrict__ pout, int nx, int ny,
-                                                      int nz, int pitch, int py, int kz, float omega, float inv_omega,
+template <int S>
+__global__ void __launch_bounds__(RX* RY) himeno_tma(const __grid_constant__ TileMaps maps, float* __restrict__ pout, int nx, int ny,
+                                                      int nz, int pitch, int py, int kz, float omega,
                                                       double* __restrict__ partials, unsigned* __restrict__ ticket,
                                                       double* __restrict__ gosa, unsigned* __restrict__ status)
 {
-    typedef TmaLayout<MODE> Lay;
-    typedef typename Lay::L L;
+    typedef TmaLayout Lay;
+    typedef float L;
     constexpr int P = S + 2;  // ring slots: planes k-1 .. k+S
     extern __shared__ __align__(128) unsigned char tsm[];
     unsigned char* stages = tsm;
@@ -399,33 +398,14 @@ __global__ void __launch_bounds__(RX* RY) himeno_tma(const __grid_constant__ Til
             const L* sp = reinterpret_cast<const L*>(slot(k + 1));
             const size_t cc = ((size_t)k * py + j) * pitch + i;
             float co[12];
-            if (MODE == 0) {
 #pragma unroll
-                for (int n = 0; n < 12; n++) co[n] = reinterpret_cast<const float*>(st + Lay::tile_off(n))[cq];
-            } else {
-#pragma unroll
-                for (int n = 0; n < 10; n++) co[n] = __half2float(reinterpret_cast<const __half*>(st + Lay::tile_off(n))[cq]);
-                co[10] = reinterpret_cast<const float*>(st + Lay::tile_off(10))[cq];
-                co[11] = __half2float(reinterpret_cast<const __half*>(st + Lay::tile_off(11))[cq]);
-            }
-#define RF(di, dj, dk) ((float)(((dk) < 0 ? sm : ((dk) > 0 ? sp : s0))[q + (di) + (dj) * Lay::W]))
-            if (MODE == 0) {
-                const float s0v = HIMENO_S0(RF, co[0], co[1], co[2], co[4], co[5], co[6], co[7], co[8], co[9], co[11]);
-                const float pc = RF(0, 0, 0);
-                const float ss = fmul(fsub(fmul(s0v, co[3]), pc), co[10]);
-                reinterpret_cast<float*>(pout)[cc] = fadd(pc, fmul(omega, ss));
-                g.add_sq(ss);
-            } else {
-                float ne = co[0] * RF(1, 0, 0) + co[1] * RF(0, 1, 0) + co[2] * RF(0, 0, 1);
-                ne += co[3] * ((RF(1, 1, 0) - RF(1, -1, 0)) - (RF(-1, 1, 0) - RF(-1, -1, 0)));
-                ne += co[4] * ((RF(0, 1, 1) - RF(0, -1, 1)) - (RF(0, 1, -1) - RF(0, -1, -1)));
-                ne += co[5] * ((RF(1, 0, 1) - RF(-1, 0, 1)) - (RF(1, 0, -1) - RF(-1, 0, -1)));
-                ne += co[6] * RF(-1, 0, 0) + co[7] * RF(0, -1, 0) + co[8] * RF(0, 0, -1);
-                const float e0 = RF(0, 0, 0);
-                const float v = e0 + omega * co[9] * (co[10] * ne - e0) + co[11];
-                reinterpret_cast<__half*>(pout)[cc] = __float2half_rn(v);
-                g.add_sq((v - e0) * inv_omega);
-            }
+            for (int n = 0; n < 12; n++) co[n] = reinterpret_cast<const float*>(st + Lay::tile_off(n))[cq];
+#define RF(di, dj, dk) (((dk) < 0 ? sm : ((dk) > 0 ? sp : s0))[q + (di) + (dj) * Lay::W])
+            const float s0v = HIMENO_S0(RF, co[0], co[1], co[2], co[4], co[5], co[6], co[7], co[8], co[9], co[11]);
+            const float pc = RF(0, 0, 0);
+            const float ss = fmul(fsub(fmul(s0v, co[3]), pc), co[10]);
+            pout[cc] = fadd(pc, fmul(omega, ss));
+            g.add_sq(ss);
 #undef RF
         }
         // everyone is done with stage s and with the slot of plane k-1: refill them with plane k+S
@@ -608,7 +588,7 @@ int plain_maps(const float* const* coef, const float* pin, int nx, int ny, int n
     for (int n = 0; n < 12; n++)
         GB_TRY(gb::tensor_map_3d(&m->m[n], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, coef[n], nx + 2, py, nz + 2, pitch, py, RX, RY));
     return gb::tensor_map_3d(&m->m[12], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pin, nx + 2, py, nz + 2, pitch, py,
-                             TmaLayout<0>::W, RY + 2);
+                             TmaLayout::W, RY + 2);
 }
 
 bool plain_tma_ok(const float* const* coef, const float* p, const float* wrk2, int pitch)
@@ -663,17 +643,17 @@ int appfis_gb_himeno(const float* const* coef, float* p, float* wrk2, int nx, in
         GB_TRY(plain_maps(coef, p, nx, ny, nz, pitch, &maps[0]));
         maps[1] = maps[0];
         GB_TRY(gb::tensor_map_3d(&maps[1].m[12], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, wrk2, nx + 2, ny + 2, nz + 2, pitch,
-                                 ny + 2, TmaLayout<0>::W, RY + 2));
+                                 ny + 2, TmaLayout::W, RY + 2));
         unsigned* status;
         GB_TRY(gb::status_word(&status));
         const int kz = balanced_kz(nz, HKZ);
         dim3 tgrd(nx / RX + 1, gb::ceil_div(ny, RY), gb::ceil_div(nz, kz));
         if (dev_gosa) GB_TRY(gosa_scratch(tgrd, &partials, &ticket, st));
-        constexpr int smem = TmaLayout<0>::smem(TMA_S_PLAIN);
-        GB_CUDA(cudaFuncSetAttribute(himeno_tma<0, TMA_S_PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        constexpr int smem = TmaLayout::smem(TMA_S_PLAIN);
+        GB_CUDA(cudaFuncSetAttribute(himeno_tma<TMA_S_PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         for (int it = 0; it < iters; it++) {
-            himeno_tma<0, TMA_S_PLAIN><<<tgrd, blk, smem, st>>>(maps[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2, kz, omega, 0.0f,
-                                                               partials, ticket, dev_gosa ? dev_gosa + it : nullptr, status);
+            himeno_tma<TMA_S_PLAIN><<<tgrd, blk, smem, st>>>(maps[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2, kz, omega, partials,
+                                                            ticket, dev_gosa ? dev_gosa + it : nullptr, status);
             ci = 1 - ci;
         }
         GB_TRY(gb::launched("himeno_tma<plain>"));

@@ -235,6 +235,45 @@ def cpu_app_samples():
     return out
 
 
+def apps_unchanged():
+    """The reference's sample applications, unchanged, on three builds on this machine: the
+    reference's CPU path (OpenMP, every core), the reference's own GPU path (APPFIS_CUDA for
+    sm_103a) and the drop-in headers (generic functor kernels of this engine; both GPU builds
+    with nvcc's default FMA contraction).  GLUP/s from each
+    application's own COMPUTE timer (its printed `Compute:` seconds)."""
+    import re
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import build_ref
+    from tests.dropin import build_apps
+
+    cases = [("HeatDiffusion", ["-dimx=256", "-dimy=256", "-dimz=256", "-iteration=100"], 256 ** 3 * 100),
+             ("GameOfLife", ["-dimx=4096", "-dimy=4096", "-iteration=200"], 4096 ** 2 * 200),
+             ("Himeno", ["-dimx=129", "-dimy=129", "-dimz=257", "-iteration=100"], 129 * 129 * 257 * 100),
+             ("FDTD3d", ["-dimx=256", "-dimy=256", "-dimz=256", "-iteration=50"], 256 ** 3 * 50)]
+    apps = [c[0] for c in cases]
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        ref = dict(zip(apps, ex.map(build_ref.app_ref_exe, apps)))
+        refgpu = dict(zip(apps, ex.map(build_ref.app_refgpu_exe, apps)))
+    gbx = build_apps.build(apps, exact=False)  # nvcc's default contraction, like the reference's GPU build
+    cores = os.cpu_count() or 1
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        for app, args, lups in cases:
+            row = {"args": " ".join(args)}
+            for name, exe, extra in (("reference_cpu", ref[app], ["-thread=%d" % cores]), ("reference_gpu", refgpu[app], []),
+                                     ("dropin_gpu", gbx[app], [])):
+                r = subprocess.run([exe] + args + extra, capture_output=True, text=True, timeout=900, cwd=td)
+                m = re.search(r"^Compute:\s*(\S+)", r.stdout, re.M)
+                if r.returncode != 0 or not m:
+                    row[name] = {"error": (r.stderr or r.stdout)[-300:]}
+                    continue
+                secs = float(m.group(1))
+                row[name] = {"compute_s": secs, "glups": lups / secs / 1e9}
+            out[app] = row
+    return {"apps_unchanged": out, "cores": cores}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -758,6 +797,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-apps", action="store_true", help="skip the per-workload measurements")
     ap.add_argument("--apps", default="heat2d,himeno,fdtd3d,flood", help="comma-separated per-workload measurements")
+    ap.add_argument("--apps-unchanged", action="store_true",
+                    help="time the reference's sample applications on its CPU path, its GPU path and the drop-in")
     ap.add_argument("--profile-case", choices=["life", "himeno", "fdtd", "heat", "flood"], default=None,
                     help="launch a short fixed sequence of the named workload's kernels (for ncu), no timing")
     args = ap.parse_args()
@@ -765,6 +806,11 @@ def main():
     rank, world, local = dist_setup(args.gpus)
     if args.profile_case:
         profile_case(args.profile_case, local)
+    elif args.apps_unchanged:
+        if rank == 0:
+            from appfis_gb300 import build as gb_build
+            gb_build.build()
+            print(json.dumps(apps_unchanged()), flush=True)
     elif args.impl == "reference":
         run_reference(args, rank, world)
     else:

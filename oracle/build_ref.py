@@ -131,6 +131,22 @@ def app_ref_exe(app):
     return exe
 
 
+def app_refgpu_exe(app):
+    """The reference's own GPU build of an application (APPFIS_CUDA for sm_103a, the MPI
+    stand-in; built on first use with nvcc), or None."""
+    src = app_source(app, "ref")
+    if not os.path.exists(src):
+        return None
+    exe = os.path.join(APPS_DIR, "%s.refgpu" % app)
+    if not (_runs_here(exe) and os.path.getmtime(exe) >= os.path.getmtime(src)):
+        cmd = ["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-x", "cu", "-DAPPFIS_CUDA=1", "-O3", "-std=c++11", "-w",
+               "-Xcompiler", "-fopenmp", src, "-o", exe, "-lgomp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("building %s failed:\n%s" % (exe, r.stderr[-4000:]))
+    return exe
+
+
 def flat_path(name):
     return os.path.join(OUT, "ref_%s.flat.cpp" % name)
 

@@ -1,11 +1,11 @@
 """Builds the reference's five sample applications, unchanged, against the drop-in headers
 (appfis_gb300/Appfis) and libappfis_gb.so, the way their makefiles build the APPFIS_CUDA
-configuration (nvcc -x cu -DAPPFIS_CUDA=1), plus -fmad=false so that the functors' multiplies
+configuration (nvcc -x cu -DAPPFIS_CUDA=1), by default plus -fmad=false so that the functors' multiplies
 and adds round separately like the reference's CPU build.
 
 The application sources come from oracle/_ref/apps/<app>.gb.cpp (flattened by
 oracle/build_ref.py from the reference tree; git-ignored, never committed).  Executables go to
-the same folder as <app>.gb; they are rebuilt when the library, the drop-in headers or the
+the same folder as <app>.gb (<app>.gbfma without -fmad=false); they are rebuilt when the library, the drop-in headers or the
 source change, or when they were built for another host architecture."""
 import os
 import platform
@@ -30,16 +30,19 @@ def _newest_input(src):
     return max(os.path.getmtime(f) for f in files)
 
 
-def build_one(app):
+def build_one(app, exact=True):
+    """exact: -fmad=false (the functors' multiplies and adds rounded separately, as on the
+    reference's CPU build); otherwise nvcc's default contraction, as the reference's own GPU
+    build uses (for timing against it)."""
     src = source(app)
-    exe = os.path.join(APPS_DIR, "%s.gb" % app)
+    exe = os.path.join(APPS_DIR, "%s.%s" % (app, "gb" if exact else "gbfma"))
     stamp = exe + ".arch"
     if (os.path.exists(exe) and os.path.exists(stamp) and open(stamp).read() == platform.machine()
             and os.path.getmtime(exe) >= _newest_input(src)):
         return exe
-    cmd = ["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-x", "cu", "-DAPPFIS_CUDA=1", "-O2", "-std=c++11",
-           "-fmad=false", "-w", "-I", os.path.join(LIBDIR, "Appfis"), "-I", os.path.join(ROOT, "include"), "-o", exe, src,
-           "-L", LIBDIR, "-lappfis_gb", "-Xlinker", "-rpath=" + LIBDIR]
+    cmd = ["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-x", "cu", "-DAPPFIS_CUDA=1", "-O3", "-std=c++11",
+           "-w", "-I", os.path.join(LIBDIR, "Appfis"), "-I", os.path.join(ROOT, "include"), "-o", exe, src,
+           "-L", LIBDIR, "-lappfis_gb", "-Xlinker", "-rpath=" + LIBDIR] + (["-fmad=false"] if exact else [])
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("building %s against the drop-in failed:\n%s" % (app, r.stderr[-4000:]))
@@ -52,6 +55,6 @@ def available():
     return all(os.path.exists(source(a)) for a in APPS)
 
 
-def build(apps=APPS):
+def build(apps=APPS, exact=True):
     with ThreadPoolExecutor(max_workers=len(apps)) as ex:
-        return dict(zip(apps, ex.map(build_one, apps)))
+        return dict(zip(apps, ex.map(lambda a: build_one(a, exact), apps)))
