@@ -571,6 +571,121 @@ __global__ void __launch_bounds__(MX / 2 * MY) himeno_mixed2(const __grid_consta
         gosa_reduce(k < k1 ? __longlong_as_double(0x7ff8000000000000ll) : (double)g.x + (double)g.y, partials, ticket, gosa);
 }
 
+// ---------------------------------------------------------------- TMA-staged correction pass
+// P' = P + e, D = omega*ss(P'), e_next = 0, on the same 32 x 8 tile and z-march as himeno_tma.
+// A stage brings the twelve FP32 coefficient tiles of plane k and the P (FP32, 40 x 10) and e
+// (FP16, 48 x 10) boxes of plane k+2; the threads add them once into an FP32 ring of Q = P + e
+// (planes k-1 .. k+2), so the 19-point sum reads shared memory only.
+struct CorrMaps {
+    CUtensorMap m[14];  // 0..11 coefficients, 12 P, 13 e
+};
+constexpr int CPB = (TmaLayout::RB + 127) / 128 * 128;  // P box slot (40 x 10 FP32)
+constexpr int CEB = 48 * (RY + 2) * 2;                   // e box bytes (48 x 10 FP16)
+constexpr int CES = (CEB + 127) / 128 * 128;
+constexpr int CSTG = TmaLayout::CT + CPB + CES;          // one stage
+constexpr int CQ = TmaLayout::W * (RY + 2);              // floats per Q ring slot
+constexpr int CORR_S = 2;
+constexpr int corr_smem(int S) { return S * CSTG + 4 * CQ * 4 + 3 * (CPB + CES) + S * 8; }
+
+// Q = P + e over one 40 x 10 box (e's box starts 4 columns further left)
+__device__ __forceinline__ void q_box(const unsigned char* pbox, const unsigned char* ebox, float* q, int t)
+{
+    const float* P = reinterpret_cast<const float*>(pbox);
+    const __half* E = reinterpret_cast<const __half*>(ebox);
+    for (int idx = t; idx < CQ; idx += RX * RY) {
+        const int r = idx / TmaLayout::W, c = idx - r * TmaLayout::W;
+        q[idx] = P[idx] + __half2float(E[r * 48 + c + 4]);
+    }
+}
+
+template <int S>
+__global__ void __launch_bounds__(RX* RY) himeno_correct_tma(const __grid_constant__ CorrMaps maps, float* __restrict__ Pn,
+                                                              __half* __restrict__ D, __half* __restrict__ ezero, int nx, int ny,
+                                                              int nz, int pitch, int py, int kz, float omega,
+                                                              unsigned* __restrict__ status)
+{
+    typedef TmaLayout Lay;
+    extern __shared__ __align__(128) unsigned char tsm[];
+    unsigned char* stages = tsm;
+    float* ring = reinterpret_cast<float*>(tsm + S * CSTG);
+    unsigned char* pro = tsm + S * CSTG + 4 * CQ * 4;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(pro + 3 * (CPB + CES));
+    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * RX + tx;
+    const int x0 = blockIdx.x * RX, y0 = 1 + blockIdx.y * RY;
+    const int i = x0 + tx, j = y0 + ty;
+    const int k0 = 1 + blockIdx.z * kz, k1 = min(k0 + kz, nz + 1);
+    const bool act = i >= 1 && i <= nx && j <= ny;
+    if (gb::tma::smem_u32(tsm) & 127u) {
+        if (t == 0) atomicOr(status, (unsigned)gb::ST_SMEM_ALIGN);
+        return;
+    }
+    if (t == 0) {
+#pragma unroll
+        for (int s = 0; s < S; s++) gb::tma::bar_init(&bar[s], 1);
+        gb::tma::fence_init();
+        for (int n = 0; n < 14; n++) gb::tma::prefetch_map(&maps.m[n]);
+    }
+    __syncthreads();
+    auto slot = [&](int pl) { return ring + ((pl - (k0 - 1)) & 3) * CQ; };
+    auto issue = [&](int k) {
+        const int s = (k - k0) % S;
+        unsigned char* st = stages + s * CSTG;
+        gb::tma::arrive_expect(&bar[s], Lay::CT + (Lay::RB + CEB) * (k == k0 ? 4 : 1));
+        if (k == k0)
+            for (int d = 0; d < 3; d++) {
+                unsigned char* b = pro + d * (CPB + CES);
+                gb::tma::load_3d(b, &maps.m[12], x0 - Lay::XO, y0 - 1, k0 - 1 + d, &bar[s]);
+                gb::tma::load_3d(b + CPB, &maps.m[13], x0 - 8, y0 - 1, k0 - 1 + d, &bar[s]);
+            }
+#pragma unroll
+        for (int n = 0; n < 12; n++) gb::tma::load_3d(st + Lay::tile_off(n), &maps.m[n], x0, y0, k, &bar[s]);
+        gb::tma::load_3d(st + Lay::CT, &maps.m[12], x0 - Lay::XO, y0 - 1, k + 2, &bar[s]);
+        gb::tma::load_3d(st + Lay::CT + CPB, &maps.m[13], x0 - 8, y0 - 1, k + 2, &bar[s]);
+    };
+    if (t == 0)
+        for (int k = k0; k < min(k0 + S, k1); k++) issue(k);
+
+    bool bad = false;
+    int k = k0;
+    const int cq = ty * RX + tx;
+    const int q = (ty + 1) * Lay::W + tx + Lay::XO;
+    for (; k < k1; k++) {
+        const int s = (k - k0) % S;
+        if (!gb::tma::wait(&bar[s], (unsigned)((k - k0) / S) & 1u)) bad = true;
+        const unsigned char* st = stages + s * CSTG;
+        if (k == k0) {  // uniform
+            for (int d = 0; d < 3; d++) q_box(pro + d * (CPB + CES), pro + d * (CPB + CES) + CPB, slot(k0 - 1 + d), t);
+            __syncthreads();
+        }
+        q_box(st + Lay::CT, st + Lay::CT + CPB, slot(k + 2), t);  // plane k+2 into the slot plane k-2 left
+        if (act && !bad) {
+            const float* sm = slot(k - 1);
+            const float* s0 = slot(k);
+            const float* sp = slot(k + 1);
+            float co[12];
+#pragma unroll
+            for (int n = 0; n < 12; n++) co[n] = reinterpret_cast<const float*>(st + Lay::tile_off(n))[cq];
+#define RF(di, dj, dk) (((dk) < 0 ? sm : ((dk) > 0 ? sp : s0))[q + (di) + (dj) * Lay::W])
+            const float s0v = HIMENO_S0(RF, co[0], co[1], co[2], co[4], co[5], co[6], co[7], co[8], co[9], co[11]);
+            const float q0 = RF(0, 0, 0);
+#undef RF
+            const float ss = (s0v * co[3] - q0) * co[10];
+            const size_t cc = ((size_t)k * py + j) * pitch + i;
+            Pn[cc] = q0;
+            D[cc] = __float2half_rn(omega * ss);
+            ezero[cc] = __float2half_rn(0.0f);
+        }
+        // everyone is done with stage s, the slot of plane k-1 and the sums of plane k+2
+        if (__syncthreads_or(bad)) break;
+        if (t == 0 && k + S < k1) issue(k + S);
+    }
+    if (k < k1 && t == 0) {  // a wait gave up: report and let the copies still in flight land
+        atomicOr(status, (unsigned)gb::ST_TMA_TIMEOUT);
+        for (int kk = k; kk < min(k + S, k1); kk++)
+            gb::tma::wait(&bar[(kk - k0) % S], (unsigned)((kk - k0) / S) & 1u, gb::tma::DRAIN_NS);
+    }
+}
+
 // z planes per CTA: about HKZ, balanced so that no chunk is much shorter than the others
 inline int balanced_kz(int nz, int target)
 {
@@ -722,11 +837,37 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     unsigned* rticket = nullptr;
     if (dev_gosa) GB_TRY(gosa_scratch(use_tma ? tgrd : rgrd, &rpartials, &rticket, st));
     float* P[2] = {p, p_work};
+    // correction maps: [P buffer][e buffer]
+    CorrMaps cmaps[2][2];
+    dim3 cgrd(nx / RX + 1, gb::ceil_div(ny, RY), gb::ceil_div(nz, tkz));
+    constexpr int csmem = corr_smem(CORR_S);
+    if (use_tma) {
+        const int py = ny + 2;
+        for (int n = 0; n < 12; n++)
+            GB_TRY(gb::tensor_map_3d(&cmaps[0][0].m[n], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, coef[n], nx + 2, py, nz + 2, pitch, py, RX, RY));
+        for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 2; b++) {
+                if (a || b) cmaps[a][b] = cmaps[0][0];
+                GB_TRY(gb::tensor_map_3d(&cmaps[a][b].m[12], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P[a], nx + 2, py, nz + 2, pitch, py,
+                                         TmaLayout::W, RY + 2));
+                GB_TRY(gb::tensor_map_3d(&cmaps[a][b].m[13], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, E[b], nx + 2, py, nz + 2, pitch, py, 48,
+                                         RY + 2));
+            }
+        GB_CUDA(cudaFuncSetAttribute(himeno_correct_tma<CORR_S>, cudaFuncAttributeMaxDynamicSharedMemorySize, csmem));
+    }
     int pc = 0, ec = 0;
-    // D from the initial P (e = 0), e restarted at 0
-    himeno_correct<HBX, HBY><<<grd, blk, 0, st>>>(cf, P[pc], E[ec], P[1 - pc], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2, HKZ, omega);
-    pc = 1 - pc;
-    ec = 1 - ec;
+    // the correction pass: P' = P + e into the other P buffer, D, the other e buffer zeroed
+    auto correct = [&]() {
+        if (use_tma)
+            himeno_correct_tma<CORR_S><<<cgrd, rblk, csmem, st>>>(cmaps[pc][ec], P[1 - pc], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2,
+                                                                 tkz, omega, status);
+        else
+            himeno_correct<HBX, HBY><<<grd, blk, 0, st>>>(cf, P[pc], E[ec], P[1 - pc], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2,
+                                                          HKZ, omega);
+        pc = 1 - pc;
+        ec = 1 - ec;
+    };
+    correct();  // D from the initial P (e = 0), e restarted at 0
     const float inv_omega = 1.0f / omega;
     for (int it = 0; it < iters; it++) {
         if (use_tma)
@@ -736,12 +877,7 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
             himeno_ring<1><<<rgrd, rblk, 0, st>>>(cf, hf, E[ec], E[1 - ec], Dd, nx, ny, nz, pitch, ny + 2, HKZ, omega, inv_omega,
                                                   rpartials, rticket, dev_gosa ? dev_gosa + it : nullptr);
         ec = 1 - ec;
-        if ((it + 1) % period == 0 || it + 1 == iters) {
-            himeno_correct<HBX, HBY><<<grd, blk, 0, st>>>(cf, P[pc], E[ec], P[1 - pc], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2,
-                                                          HKZ, omega);
-            pc = 1 - pc;
-            ec = 1 - ec;
-        }
+        if ((it + 1) % period == 0 || it + 1 == iters) correct();
     }
     GB_TRY(gb::launched("himeno_mixed"));
     if (cur_index) *cur_index = pc;
