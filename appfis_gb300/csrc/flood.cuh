@@ -114,7 +114,7 @@ __device__ void phase_a(const Dom<T> D, Ctl* ctl, int cur, int d, long long loca
 {
     const int lane = threadIdx.x & 31;
     const int sx = (int)(local % D.strips_x), sy = (int)(local / D.strips_x);
-    const int i = 1 + sx * 32 + lane;
+    const int i = sx * SCOLS + lane;  // lanes 1..SCOLS: the strip's interior columns
     const int j0 = 1 + sy * ROWS, j1 = min(j0 + ROWS, D.ny + 1);
     const T* __restrict__ h = D.h[b];
     T* __restrict__ qx = D.qx[b];
@@ -124,7 +124,7 @@ __device__ void phase_a(const Dom<T> D, Ctl* ctl, int cur, int d, long long loca
     const T hextra = (T)p.hextra, E = K<T>::dry(), G = K<T>::g();
     const T dx = (T)p.dx, cn = (T)p.cn;
     T mn = K<T>::big();  // min in T (exact), widened once per warp: no per-cell FP64 work in float
-    if (i <= D.nx) {
+    if (lane >= 1 && lane <= SCOLS && i <= D.nx) {
         for (int jb = j0; jb < j1; jb += FA_ROWS) {
             T hv[FA_ROWS], qxv[FA_ROWS], qyv[FA_ROWS];
 #pragma unroll
@@ -194,16 +194,20 @@ __device__ __forceinline__ Cell<T> cell_of(const Raw<T>& r)
     return make_cell<T>(r.h, r.qx, r.qy, r.z);
 }
 
-// Each warp marches its strip's rows; the loads of row j+2 (and the lane-0 / lane-31 neighbour
-// cells of row j+1) are issued while row j is computed.
+// Each warp marches its strip's rows.  Lane l holds column 30*sx + l of the row: lanes 1..30 are
+// the strip's interior cells, lanes 0 and 31 the neighbour columns, so one coalesced row load
+// brings every cell the strip's faces need.  Lanes 0..30 compute the X face between their cell
+// and the next lane's (lane 0's is the strip's left face), lanes 1..30 the Y faces and updates.
+// The loads of row j+2 are issued while row j is computed.
 template <class T>
 __device__ void phase_b(const Dom<T> D, long long local, int b, T dt, const Params& p)
 {
     const int lane = threadIdx.x & 31;
     const int sx = (int)(local % D.strips_x), sy = (int)(local / D.strips_x);
-    const int i = 1 + sx * 32 + lane;
+    const int i = sx * SCOLS + lane;
     const int j0 = 1 + sy * ROWS, j1 = min(j0 + ROWS, D.ny + 1);
-    const bool act = i <= D.nx;
+    const bool own = lane >= 1 && lane <= SCOLS && i <= D.nx;  // cells this lane updates
+    const bool xface = lane <= SCOLS && i <= D.nx;             // face i|i+1 is needed
     const T dx = (T)p.dx, hextra = (T)p.hextra;
     const T one = T(1), zero = T(0);
     const T* __restrict__ h = D.h[b];
@@ -219,49 +223,33 @@ __device__ void phase_b(const Dom<T> D, long long local, int b, T dt, const Para
 
     Cell<T> cj = cell_of(load_raw(h, qx, qy, dem, px, nx, i, j0));
     Raw<T> rn = load_raw(h, qx, qy, dem, px, nx, i, j0 + 1);  // rows j0+1 <= ny+1 always exist
-    Raw<T> side = zr;                                           // lane 31: cell i+1, lane 0: cell i-1 of row j
-    if (lane == 31) side = load_raw(h, qx, qy, dem, px, nx, i + 1, j0);
-    if (lane == 0) side = load_raw(h, qx, qy, dem, px, nx, i - 1, j0);
     T ycar[3] = {zero, zero, zero};  // rhs0 Y part of row j (from face j|j-1)
     bool ywet = false;
-    if (act) {
+    if (own) {
         const Cell<T> cm = cell_of(load_raw(h, qx, qy, dem, px, nx, i, j0 - 1));
         T r2[3];
         ywet = face<T>(cj, cm, zero, one, dx, dt, hextra, ycar, r2);
     }
     for (int j = j0; j < j1; j++) {
-        // prefetch: row j+2, the side cell of row j+1, this cell's n^2
-        const Raw<T> rnn = j + 2 <= ny + 1 ? load_raw(h, qx, qy, dem, px, nx, i, j + 2) : zr;
-        Raw<T> sidn = zr;
-        if (j + 1 < j1) {
-            if (lane == 31) sidn = load_raw(h, qx, qy, dem, px, nx, i + 1, j + 1);
-            if (lane == 0) sidn = load_raw(h, qx, qy, dem, px, nx, i - 1, j + 1);
-        }
+        const Raw<T> rnn = j + 2 <= ny + 1 ? load_raw(h, qx, qy, dem, px, nx, i, j + 2) : zr;  // prefetch
         const size_t c = (size_t)j * px + i;
-        const T n2v = act ? n2[c] : zero;
+        const T n2v = own ? n2[c] : zero;
         const Cell<T> cn_ = cell_of(rn);
-        // X face i|i+1 of row j
-        Cell<T> right = shfl_cell(cj, 1, true);
-        if (lane == 31 && act) right = cell_of(side);
+        // X face i|i+1 of row j: rhs0 of cell i, rhs1 of cell i+1 (the next lane)
+        const Cell<T> right = shfl_cell(cj, 1, true);
         T xr1[3] = {zero, zero, zero}, xr2[3] = {zero, zero, zero};
         bool xwet = false;
-        if (act) xwet = face<T>(cj, right, one, zero, dx, dt, hextra, xr1, xr2);
-        // rhs1 X part of cell i comes from face i-1|i (left lane, or computed by lane 0)
+        if (xface) xwet = face<T>(cj, right, one, zero, dx, dt, hextra, xr1, xr2);
         T lr[3];
-        bool lwet;
         lr[0] = __shfl_up_sync(0xffffffffu, xr2[0], 1);
         lr[1] = __shfl_up_sync(0xffffffffu, xr2[1], 1);
         lr[2] = __shfl_up_sync(0xffffffffu, xr2[2], 1);
-        lwet = __shfl_up_sync(0xffffffffu, (int)xwet, 1) != 0;
-        if (lane == 0 && act) {
-            T t1[3];
-            lwet = face<T>(cell_of(side), cj, one, zero, dx, dt, hextra, t1, lr);
-        }
+        const bool lwet = __shfl_up_sync(0xffffffffu, (int)xwet, 1) != 0;
         // Y face j+1|j: id1 = row j+1, id2 = row j
         T yn1[3] = {zero, zero, zero}, yr2[3] = {zero, zero, zero};
         bool ynwet = false;
-        if (act) ynwet = face<T>(cn_, cj, zero, one, dx, dt, hextra, yn1, yr2);
-        if (act) {
+        if (own) ynwet = face<T>(cn_, cj, zero, one, dx, dt, hextra, yn1, yr2);
+        if (own) {
             T r0[3], r1[3];
 #pragma unroll
             for (int k = 0; k < 3; k++) {
@@ -281,7 +269,6 @@ __device__ void phase_b(const Dom<T> D, long long local, int b, T dt, const Para
         ywet = ynwet;
         cj = cn_;
         rn = rnn;
-        side = sidn;
     }
 }
 

@@ -34,6 +34,7 @@
 namespace flood {
 
 constexpr int ROWS = 32;        // rows per strip
+constexpr int SCOLS = 30;       // interior columns per strip (a warp's lanes 1..30; lanes 0 and 31 hold the halo)
 constexpr int MAXD = 64;        // domains per batch
 
 template <class T> struct K;

@@ -82,7 +82,7 @@ int make_table(const appfis_gb_flood_domain* doms, int ndom, std::vector<Dom<T>>
         D.nx = s.nx;
         D.ny = s.ny;
         D.px = s.pitch;
-        D.strips_x = (s.nx + 31) / 32;
+        D.strips_x = (s.nx + SCOLS - 1) / SCOLS;
         D.strip0 = total;
         total += (long long)D.strips_x * ((s.ny + ROWS - 1) / ROWS);
     }
