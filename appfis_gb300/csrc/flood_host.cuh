@@ -187,8 +187,8 @@ int job(int ndom, const int* nx, const int* ny, const double* const* dem, double
         double* dtlog_host)
 {
     if (ndom < 1 || ndom > MAXD || !nx || !ny || !dem || !h || !prm) return gb::fail(APPFIS_GB_EINVAL, "flood_job: bad arguments");
-    static cudaStream_t st = nullptr;
-    if (!st) GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cudaStream_t st;
+    GB_TRY(gb::job_stream(&st));
     std::vector<appfis_gb_flood_domain> doms(ndom);
     std::vector<size_t> off(ndom);
     size_t fields_elems = 0, max_int = 0;

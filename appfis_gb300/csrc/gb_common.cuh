@@ -35,6 +35,9 @@ inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b
 // Number of SMs of the current device (cached).
 int sm_count();
 
+// The non-blocking stream the _job entry points run on, one per device (created on first use).
+int job_stream(cudaStream_t* out);
+
 #define GB_TRY(expr)                 \
     do {                             \
         int _st = (expr);            \

@@ -44,6 +44,7 @@ std::vector<std::vector<Buf>> g_dev;  // [device][slot]
 Buf g_pinned[2];
 std::vector<int> g_sms;
 std::vector<unsigned*> g_status;  // [device]
+std::vector<cudaStream_t> g_job_streams;  // [device]
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 std::once_flag g_encode_once;
 }  // namespace
@@ -101,6 +102,17 @@ int sm_count()
         g_sms[dev] = n;
     }
     return g_sms[dev];
+}
+
+int job_stream(cudaStream_t* out)
+{
+    int dev = 0;
+    GB_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_mu);
+    if ((int)g_job_streams.size() <= dev) g_job_streams.resize(dev + 1, nullptr);
+    if (!g_job_streams[dev]) GB_CUDA(cudaStreamCreateWithFlags(&g_job_streams[dev], cudaStreamNonBlocking));
+    *out = g_job_streams[dev];
+    return APPFIS_GB_OK;
 }
 
 int status_word(unsigned** out)

@@ -127,11 +127,7 @@ int appfis_gb_heat2d(float* a, float* b, int nx, int ny, int pitch, int iters, f
     if (iters < 0) return gb::fail(APPFIS_GB_EINVAL, "heat2d: negative iteration count");
     cudaStream_t st = gb::as_stream(stream);
     constexpr size_t smem = sizeof(float) * 2 * (HTX + 2 * HSMAX) * (HTY + 2 * HSMAX);
-    static bool configured = false;
-    if (!configured) {
-        GB_CUDA(cudaFuncSetAttribute(heat2d_blocked<HTX, HTY, HSMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
+    GB_CUDA(cudaFuncSetAttribute(heat2d_blocked<HTX, HTY, HSMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grd(gb::ceil_div(nx, HTX), gb::ceil_div(ny, HTY));
     float* buf[2] = {a, b};
     int ci = 0;
@@ -149,8 +145,8 @@ int appfis_gb_heat2d(float* a, float* b, int nx, int ny, int pitch, int iters, f
 int appfis_gb_heat2d_job(float* field, int nx, int ny, int iters, float cx, float cy, double* stats)
 {
     if (!field || nx < 1 || ny < 1 || iters < 0) return gb::fail(APPFIS_GB_EINVAL, "heat2d_job: bad arguments");
-    static cudaStream_t st = nullptr;
-    if (!st) GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cudaStream_t st;
+    GB_TRY(gb::job_stream(&st));
     const int px = nx + 2, py = ny + 2;
     const size_t bytes = sizeof(float) * (size_t)px * py;
     void *a, *b, *res;

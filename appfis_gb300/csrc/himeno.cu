@@ -890,8 +890,8 @@ int appfis_gb_himeno_job(const float* coef_host, float* p_host, int nx, int ny, 
     if (!coef_host || !p_host) return gb::fail(APPFIS_GB_EINVAL, "himeno_job: null input");
     if (form != 0 && form != 1) return gb::fail(APPFIS_GB_EINVAL, "himeno_job: form %d", form);
     GB_TRY(check_dims(nx, ny, nz, nx + 2));
-    static cudaStream_t st = nullptr;
-    if (!st) GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cudaStream_t st;
+    GB_TRY(gb::job_stream(&st));
     const size_t field = (size_t)(nx + 2) * (ny + 2) * (nz + 2);
     void *dc, *da, *db, *dh, *dg;
     GB_TRY(gb::workspace(gb::WS_JOB_A, sizeof(float) * 12 * field, &dc));
@@ -915,7 +915,7 @@ int appfis_gb_himeno_job(const float* coef_host, float* p_host, int nx, int ny, 
     GB_CUDA(cudaMemcpyAsync(p_host, ci == 0 ? da : db, sizeof(float) * field, cudaMemcpyDeviceToHost, st));
     if (gosa_host && iters > 0) GB_CUDA(cudaMemcpyAsync(gosa_host, dg, sizeof(double) * iters, cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
-    return APPFIS_GB_OK;
+    return gb::check_status("himeno_job");
 }
 
 }  // extern "C"

@@ -575,8 +575,8 @@ int appfis_gb_life_job(const uint8_t* cells_in, uint8_t* cells_out, int nx, int 
     if (form != APPFIS_GB_FORM_U8 && form != APPFIS_GB_FORM_BITS) return gb::fail(APPFIS_GB_EINVAL, "life_job: form %d", form);
     GB_TRY(check_life(cells_in, cells_in + 1, nx, ny, gens, rule));
     if (form == APPFIS_GB_FORM_BITS && nx % 32) return gb::fail(APPFIS_GB_EINVAL, "life_job: bit form needs nx %% 32 == 0");
-    static cudaStream_t st = nullptr;
-    if (!st) GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cudaStream_t st;
+    GB_TRY(gb::job_stream(&st));
     const size_t n = (size_t)nx * ny;
     const size_t nbytes = (n + 15) & ~(size_t)15;
     void *ua, *ub, *cnt;
