@@ -61,11 +61,14 @@ class FloodDomain(ctypes.Structure):
 class FloodParams(ctypes.Structure):
     """appfis_gb_flood_params"""
     _fields_ = [("dx", _d), ("courant", _d), ("hextra", _d), ("t_end", _d), ("print_interval", _d),
-                ("time_step", _d), ("t_start", _d), ("max_steps", _i)]
+                ("time_step", _d), ("t_start", _d), ("max_steps", _i), ("flags", _i)]
+
+
+FLOOD_SKIP_DRY = 1
 
 
 def flood_job(domains, dx, courant, hextra, manning, t_end, print_interval=None, time_step=1.0, max_steps=0,
-              dtype=F32, qx=None, qy=None):
+              dtype=F32, qx=None, qy=None, flags=0):
     """Run a batch of flood domains from host arrays.  domains: list of (dem, h) FP64 (ny, nx)
     arrays.  Returns dict(h=[...], qx=[...], qy=[...], steps=[...], mass=[(m0, m1)], dts=[...])."""
     import numpy as np
@@ -78,7 +81,7 @@ def flood_job(domains, dx, courant, hextra, manning, t_end, print_interval=None,
     qys = [np.zeros_like(a) if qy is None else np.ascontiguousarray(qy[k], dtype=np.float64).copy() for k, a in enumerate(hs)]
     P = lambda arrs: (_P * nd)(*[a.ctypes.data for a in arrs])
     prm = FloodParams(dx, courant, hextra, t_end, t_end if print_interval is None else print_interval, time_step, 0.0,
-                      max_steps)
+                      max_steps, flags)
     steps = (_i * nd)()
     mass = (_d * (2 * nd))()
     dtlog = np.zeros(nd * max(max_steps, 1), dtype=np.float64)

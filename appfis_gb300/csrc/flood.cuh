@@ -41,6 +41,7 @@ struct Params {
     int max_steps, ndom;
     long long total_strips;
     double* dtlog;  // [ndom][max_steps] or null
+    unsigned char* zc;  // [2][total_strips] dry-step counters (null: every strip every step)
 };
 
 constexpr unsigned long long SPIN_LIMIT = 1ull << 25;
@@ -200,7 +201,7 @@ __device__ __forceinline__ Cell<T> cell_of(const Raw<T>& r)
 // and the next lane's (lane 0's is the strip's left face), lanes 1..30 the Y faces and updates.
 // The loads of row j+2 are issued while row j is computed.
 template <class T>
-__device__ void phase_b(const Dom<T> D, long long local, int b, T dt, const Params& p)
+__device__ bool phase_b(const Dom<T> D, long long local, int b, T dt, const Params& p)
 {
     const int lane = threadIdx.x & 31;
     const int sx = (int)(local % D.strips_x), sy = (int)(local / D.strips_x);
@@ -220,6 +221,7 @@ __device__ void phase_b(const Dom<T> D, long long local, int b, T dt, const Para
     T* __restrict__ qyo_ = D.qy[1 - b];
     const int px = D.px, nx = D.nx, ny = D.ny;
     const Raw<T> zr = {zero, zero, zero, zero};
+    bool dry = true;  // every cell this lane updated ends with h = qx = qy = 0
 
     Cell<T> cj = cell_of(load_raw(h, qx, qy, dem, px, nx, i, j0));
     Raw<T> rn = load_raw(h, qx, qy, dem, px, nx, i, j0 + 1);  // rows j0+1 <= ny+1 always exist
@@ -263,6 +265,7 @@ __device__ void phase_b(const Dom<T> D, long long local, int b, T dt, const Para
             ho_[c] = hn;
             qxo_[c] = qxn;
             qyo_[c] = qyn;
+            dry = dry && hn == zero && qxn == zero && qyn == zero;
         }
 #pragma unroll
         for (int k = 0; k < 3; k++) ycar[k] = yn1[k];
@@ -270,6 +273,25 @@ __device__ void phase_b(const Dom<T> D, long long local, int b, T dt, const Para
         cj = cn_;
         rn = rnn;
     }
+    return __all_sync(0xffffffffu, dry);
+}
+
+// Dry-strip bookkeeping (Params::zc): zc[parity][s] counts the consecutive steps whose output of
+// strip s was entirely dry (capped at 2).  Strip s may be left out of a step when it has been
+// dry for two steps (both state buffers hold zeros there) and its four neighbour strips of the
+// same domain are dry in the step's input.
+template <class T>
+__device__ __forceinline__ bool strip_idle(const Dom<T>& D, const unsigned char* zin, long long s)
+{
+    if (zin[s] < 2) return false;
+    const long long local = s - D.strip0;
+    const int sx = (int)(local % D.strips_x), sy = (int)(local / D.strips_x);
+    const int sy_n = (D.ny + ROWS - 1) / ROWS;
+    if (sx > 0 && zin[s - 1] == 0) return false;
+    if (sx + 1 < D.strips_x && zin[s + 1] == 0) return false;
+    if (sy > 0 && zin[s - D.strips_x] == 0) return false;
+    if (sy + 1 < sy_n && zin[s + D.strips_x] == 0) return false;
+    return true;
 }
 
 // Per-domain control of a phase (state buffer, fix / dt / step flags, the step's dt), evaluated
@@ -286,7 +308,9 @@ struct DomCtl {
 #define FLOOD_F32_MIN_BLOCKS 3
 #endif
 
-template <class T>
+// SKIP: dry strips are left out (Params::zc set); a separate instantiation, so the full sweep
+// carries none of the bookkeeping.
+template <class T, bool SKIP>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1) flood_persistent(const Dom<T>* __restrict__ gdoms, Ctl* ctl,
                                                                                 Params p)
 {
@@ -296,6 +320,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
     __syncthreads();
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
     const double big = (double)K<T>::big();
 
     for (int n = 0;; n++) {
@@ -311,6 +336,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
         for (long long s = warp; s < p.total_strips; s += nwarps) {
             const int d = find_domain(doms, p.ndom, s);
             const int f = dc.flags[d];
+            if (SKIP && p.zc[(size_t)cur * p.total_strips + s] >= 1) continue;  // dry input: no fix, no dt
             if (f & 6) phase_a<T>(doms[d], ctl, cur, d, s - doms[d].strip0, f & 1, (f & 2) != 0, (f & 4) != 0, p);
         }
         if (!grid_barrier(ctl)) return;
@@ -336,7 +362,19 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
         for (long long s = warp; s < p.total_strips; s += nwarps) {
             const int d = find_domain(doms, p.ndom, s);
             const int f = dc.flags[d];
-            if (f & 4) phase_b<T>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p);
+            if (SKIP) {
+                const unsigned char* zin = p.zc + (size_t)cur * p.total_strips;
+                unsigned char* zout = p.zc + (size_t)(1 - cur) * p.total_strips;
+                const unsigned char z = zin[s];
+                if (!(f & 4) || strip_idle(doms[d], zin, s)) {  // unchanged state
+                    if (lane == 0) zout[s] = z;
+                    continue;
+                }
+                const bool dry = phase_b<T>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p);
+                if (lane == 0) zout[s] = dry ? (unsigned char)(z < 2 ? z + 1 : 2) : 0;
+            } else if (f & 4) {
+                phase_b<T>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p);
+            }
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) {  // commit the per-domain scalars of step n
             for (int d = 0; d < p.ndom; d++) {

@@ -136,10 +136,18 @@ int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_para
     p.ndom = ndom;
     p.total_strips = total;
     p.dtlog = prm->max_steps > 0 ? dev_dtlog : nullptr;
+    p.zc = nullptr;
+    if (prm->flags & APPFIS_GB_FLOOD_SKIP_DRY) {
+        void* z;
+        GB_TRY(gb::workspace(gb::WS_FLOOD_Z, 2 * (size_t)total, &z));
+        GB_CUDA(cudaMemsetAsync(z, 0, 2 * (size_t)total, st));
+        p.zc = reinterpret_cast<unsigned char*>(z);
+    }
 
     int dev = 0, per_sm = 0;
     GB_CUDA(cudaGetDevice(&dev));
-    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, flood_persistent<T>, 256, 0));
+    auto kern = p.zc ? flood_persistent<T, true> : flood_persistent<T, false>;
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
     if (per_sm < 1) return gb::fail(APPFIS_GB_ECUDA, "flood: kernel cannot be resident");
     long long want = (total * 32 + 255) / 256;  // one warp per strip at most
     int grid = (int)std::min<long long>(want, (long long)per_sm * gb::sm_count());
@@ -155,7 +163,7 @@ int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_para
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     const Dom<T>* cdt = dtab;
-    GB_CUDA(cudaLaunchKernelEx(&cfg, flood_persistent<T>, cdt, ctl, p));
+    GB_CUDA(cudaLaunchKernelEx(&cfg, kern, cdt, ctl, p));
     flood_results<<<1, MAXD, 0, st>>>(ctl, ndom, dev_steps, dev_simtime, dev_status);
     return gb::launched("flood_results");
 }

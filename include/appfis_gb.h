@@ -227,7 +227,15 @@ typedef struct {
     double time_step;      /* dt used while no cell is wet */
     double t_start;        /* initial simulated time */
     int max_steps;         /* 0 = no limit; > 0 also enables the dt log */
+    int flags;             /* APPFIS_GB_FLOOD_SKIP_DRY or 0 */
 } appfis_gb_flood_params;
+
+/* flags: strips (30 x 32 cells) whose depth and momentum are exactly 0 and whose four neighbour
+ * strips are dry as well are left out of a step: such cells cannot change (no face of theirs
+ * has water on either side), so every field is bit-identical to the full sweep.  A strip is
+ * skipped only after its output was dry for two consecutive steps (both state buffers hold the
+ * dry state). */
+#define APPFIS_GB_FLOOD_SKIP_DRY 1
 
 #define APPFIS_GB_FLOOD_MAX_DOMAINS 64
 

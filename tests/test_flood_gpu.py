@@ -75,3 +75,17 @@ def test_fp32_form_error(gb, torch_cuda):
     assert np.abs(r["h"][0] - o["h"]).sum() < 0.02 * o["h"].sum()
     m0, m1 = r["mass"][0]
     assert abs((m1 - m0) - (o["h"].sum() - h.sum())) <= 1e-5 * m0
+
+
+@pytest.mark.parametrize("dtype", [_lib.F32, _lib.F64])
+def test_skip_dry_strips_bit_identical(gb, torch_cuda, dtype):
+    """Leaving out exactly dry strips changes no field, step or dt (three domains of uneven
+    sizes, some strips never reached by the water, 150 steps)."""
+    doms = [W.triton_domain(97, 130, 11), W.triton_domain(64, 61, 12), W.triton_domain(150, 40, 13)]
+    full = _lib.flood_job(doms, 10.0, 0.5, 1e-3, 0.035, 600.0, 600.0, 1.0, max_steps=150, dtype=dtype)
+    skip = _lib.flood_job(doms, 10.0, 0.5, 1e-3, 0.035, 600.0, 600.0, 1.0, max_steps=150, dtype=dtype,
+                          flags=_lib.FLOOD_SKIP_DRY)
+    assert full["steps"] == skip["steps"]
+    for k in range(len(doms)):
+        assert np.array_equal(full["h"][k], skip["h"][k])
+        assert np.array_equal(full["dts"][k], skip["dts"][k])

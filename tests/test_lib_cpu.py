@@ -40,3 +40,11 @@ def test_version(L):
 def test_bad_arguments_are_rejected(L, call):
     assert call(L) == _lib.EINVAL
     assert len(L.appfis_gb_last_error()) > 0
+
+
+def test_flood_param_struct_layout():
+    """appfis_gb_flood_params: 7 doubles, max_steps, flags (64 bytes with natural alignment)."""
+    from appfis_gb300 import _lib
+    import ctypes
+    assert ctypes.sizeof(_lib.FloodParams) == 64
+    assert _lib.FloodParams.flags.offset == 60
