@@ -892,27 +892,31 @@ int appfis_gb_himeno_job(const float* coef_host, float* p_host, int nx, int ny, 
     GB_TRY(check_dims(nx, ny, nz, nx + 2));
     cudaStream_t st;
     GB_TRY(gb::job_stream(&st));
-    const size_t field = (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+    // device rows padded to a multiple of 8 elements (16-byte FP32 and FP16 rows: the TMA-staged
+    // kernels); host rows are dense
+    const int dense = nx + 2, pitch = (dense + 7) / 8 * 8;
+    const size_t rows = (size_t)(ny + 2) * (nz + 2), field = (size_t)pitch * rows;
+    const size_t hrow = sizeof(float) * dense, drow = sizeof(float) * pitch;
     void *dc, *da, *db, *dh, *dg;
     GB_TRY(gb::workspace(gb::WS_JOB_A, sizeof(float) * 12 * field, &dc));
     GB_TRY(gb::workspace(gb::WS_JOB_B, sizeof(float) * field, &da));
     GB_TRY(gb::workspace(gb::WS_JOB_C, sizeof(float) * field, &db));
     GB_TRY(gb::workspace(gb::WS_JOB_E, sizeof(double) * (iters > 0 ? iters : 1), &dg));
-    GB_CUDA(cudaMemcpyAsync(dc, coef_host, sizeof(float) * 12 * field, cudaMemcpyHostToDevice, st));
-    GB_CUDA(cudaMemcpyAsync(da, p_host, sizeof(float) * field, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpy2DAsync(dc, drow, coef_host, hrow, hrow, 12 * rows, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpy2DAsync(da, drow, p_host, hrow, hrow, rows, cudaMemcpyHostToDevice, st));
     GB_CUDA(cudaMemcpyAsync(db, da, sizeof(float) * field, cudaMemcpyDeviceToDevice, st));  // ghost ring in both
     const float* cp[12];
     for (int n = 0; n < 12; n++) cp[n] = reinterpret_cast<const float*>(dc) + n * field;
     int ci = 0;
     if (form == 0) {
-        GB_TRY(appfis_gb_himeno(cp, (float*)da, (float*)db, nx, ny, nz, nx + 2, iters, omega, gosa_host ? (double*)dg : nullptr,
+        GB_TRY(appfis_gb_himeno(cp, (float*)da, (float*)db, nx, ny, nz, pitch, iters, omega, gosa_host ? (double*)dg : nullptr,
                                 &ci, st));
     } else {
         GB_TRY(gb::workspace(gb::WS_JOB_D, sizeof(__half) * 13 * field, &dh));
-        GB_TRY(appfis_gb_himeno_mixed(cp, (float*)da, (float*)db, dh, nx, ny, nz, nx + 2, iters, period, omega,
+        GB_TRY(appfis_gb_himeno_mixed(cp, (float*)da, (float*)db, dh, nx, ny, nz, pitch, iters, period, omega,
                                       gosa_host ? (double*)dg : nullptr, &ci, st));
     }
-    GB_CUDA(cudaMemcpyAsync(p_host, ci == 0 ? da : db, sizeof(float) * field, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaMemcpy2DAsync(p_host, hrow, ci == 0 ? da : db, drow, hrow, rows, cudaMemcpyDeviceToHost, st));
     if (gosa_host && iters > 0) GB_CUDA(cudaMemcpyAsync(gosa_host, dg, sizeof(double) * iters, cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
     return gb::check_status("himeno_job");
