@@ -114,7 +114,7 @@ __device__ void phase_a(const Dom<T> D, Ctl* ctl, int cur, int d, long long loca
                         const Params& p)
 {
     const int lane = threadIdx.x & 31;
-    const int sx = (int)(local % D.strips_x), sy = (int)(local / D.strips_x);
+    const int loc = (int)local, sy = loc / D.strips_x, sx = loc - sy * D.strips_x;  // 32-bit: a domain has < 2^31 strips
     const int i = sx * SCOLS + lane;  // lanes 1..SCOLS: the strip's interior columns
     const int j0 = 1 + sy * ROWS, j1 = min(j0 + ROWS, D.ny + 1);
     const T* __restrict__ h = D.h[b];
@@ -204,7 +204,7 @@ template <class T>
 __device__ bool phase_b(const Dom<T> D, long long local, int b, T dt, const Params& p)
 {
     const int lane = threadIdx.x & 31;
-    const int sx = (int)(local % D.strips_x), sy = (int)(local / D.strips_x);
+    const int loc = (int)local, sy = loc / D.strips_x, sx = loc - sy * D.strips_x;  // 32-bit: a domain has < 2^31 strips
     const int i = sx * SCOLS + lane;
     const int j0 = 1 + sy * ROWS, j1 = min(j0 + ROWS, D.ny + 1);
     const bool own = lane >= 1 && lane <= SCOLS && i <= D.nx;  // cells this lane updates
@@ -285,7 +285,7 @@ __device__ __forceinline__ bool strip_idle(const Dom<T>& D, const unsigned char*
 {
     if (zin[s] < 2) return false;
     const long long local = s - D.strip0;
-    const int sx = (int)(local % D.strips_x), sy = (int)(local / D.strips_x);
+    const int loc = (int)local, sy = loc / D.strips_x, sx = loc - sy * D.strips_x;  // 32-bit: a domain has < 2^31 strips
     const int sy_n = (D.ny + ROWS - 1) / ROWS;
     if (sx > 0 && zin[s - 1] == 0) return false;
     if (sx + 1 < D.strips_x && zin[s + 1] == 0) return false;
