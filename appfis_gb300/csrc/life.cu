@@ -10,9 +10,11 @@
 // generation, Appfis/Communication.hpp:612-678) becomes index wrap-around inside the sweep.
 //
 // Layout: interior cells only, x fastest, row pitch nx bytes (u8) or nx/32 words (bits).
-// Both sweeps march down a strip of rows per warp, keeping the row above / at / below in
-// registers (each row is loaded once per warp task) and exchanging the words at lane
-// boundaries with warp shuffles; only the two end lanes load one extra word per row.
+// The one-generation sweeps (life_u8_swar, life_bits_sweep) march down a strip of rows per warp,
+// keeping the row above / at / below in registers (each row is loaded once per warp task) and
+// exchanging the words at lane boundaries with warp shuffles; only the two end lanes load one
+// extra word per row.  Runs of 16 or more bit-packed generations use life_bits_tb, which
+// advances a tile held in shared memory by 16 generations per launch.
 #include "gb_common.cuh"
 
 namespace {

@@ -4,12 +4,16 @@
 //     val = c; for a in 1..4: val += (x-a + x+a) + (y-a + y+a) + (z-a + z+a); val *= coeff
 // run once per time step by Execute3D -> Kernel3D with 8x8x4 blocks that read 25 points each.
 //
-// Here a CTA owns a 32 x (8*RY) tile of (x, y) columns and a chunk of z planes.  Each thread
-// keeps the 9 z-values of its RY columns in registers (the queue shifts by one plane per
-// step, so every input plane is read from memory once per CTA), writes its current plane
-// into a shared tile, four edge groups fetch the 4-wide x/y halo of that plane, and the x/y
-// neighbours come from shared memory.  Per point: one load, one store (8 B/LUP at FP32,
-// 4 B/LUP at FP16 storage) plus the halo and z-chunk overlap.
+// Every tile is a 2.5-D march: a CTA owns an (x, y) tile and a chunk of z planes, each thread
+// keeps the 9 z-values of its columns in registers (the queue shifts by one plane per step, so
+// every input plane is read from memory once per CTA) and the x/y neighbours come from a plane
+// held in shared memory.  Per point: one load, one store (8 B/LUP at FP32, 4 B/LUP at FP16
+// storage) plus the halo and z-chunk overlap.  Tiles (APPFIS_GB_STAR_*):
+//   star_r4_tma    (TMA_X4 / TMA_X2) planes moved by the tensor memory accelerator into an
+//                  mbarrier ring, 4 or 2 x points x 2 rows per thread, packed FP32-pair math;
+//                  needs 16-byte rows (the default whenever they are);
+//   star_r4_vec    (VEC) 4 x points per thread, register-staged plane loads;
+//   star_r4_sweep  (SCALAR2 / SCALAR4) one x point, 2 or 4 rows per thread, any pitch.
 //
 // MODE 0: the reference form (uniform coefficient, same addition order as the reference, so
 //         FP32 results are bit-identical to its CPU path).
