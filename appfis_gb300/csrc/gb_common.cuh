@@ -32,6 +32,14 @@ int pinned(int slot, size_t bytes, void** out);
 
 inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
 
+// Splits n planes into the fewest chunks of at most `target` planes, all of (nearly) equal size,
+// and returns the chunk size.
+inline int balanced_chunk(int n, int target)
+{
+    const int chunks = (n + target - 1) / target;
+    return (n + chunks - 1) / chunks;
+}
+
 // Number of SMs of the current device (cached).
 int sm_count();
 

@@ -686,13 +686,7 @@ __global__ void __launch_bounds__(RX* RY) himeno_correct_tma(const __grid_consta
     }
 }
 
-// z planes per CTA: about HKZ, balanced so that no chunk is much shorter than the others
-inline int balanced_kz(int nz, int target)
-{
-    const int chunks = (nz + target - 1) / target;
-    return (nz + chunks - 1) / chunks;
-}
-
+// HKZ: z planes per CTA (nz is split into equal chunks of at most HKZ planes)
 constexpr int HBX = 32, HBY = 4, HKZ = 32;
 constexpr int TMA_S_PLAIN = 3;
 
@@ -761,7 +755,7 @@ int appfis_gb_himeno(const float* const* coef, float* p, float* wrk2, int nx, in
                                  ny + 2, TmaLayout::W, RY + 2));
         unsigned* status;
         GB_TRY(gb::status_word(&status));
-        const int kz = balanced_kz(nz, HKZ);
+        const int kz = gb::balanced_chunk(nz, HKZ);
         dim3 tgrd(nx / RX + 1, gb::ceil_div(ny, RY), gb::ceil_div(nz, kz));
         if (dev_gosa) GB_TRY(gosa_scratch(tgrd, &partials, &ticket, st));
         constexpr int smem = TmaLayout::smem(TMA_S_PLAIN);
@@ -815,7 +809,7 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     // TMA-staged inner sweeps (two points per thread) when the FP16 rows are 16-byte aligned
     // (pitch a multiple of 8)
     const bool use_tma = pitch % 8 == 0 && gb::aligned16(hw) && gb::aligned16(coef[3]);
-    const int tkz = balanced_kz(nz, HKZ);
+    const int tkz = gb::balanced_chunk(nz, HKZ);
     dim3 tblk(MX / 2, MY), tgrd(nx / MX + 1, gb::ceil_div(ny, MY), gb::ceil_div(nz, tkz));
     TileMaps tmaps[2];
     unsigned* status = nullptr;
