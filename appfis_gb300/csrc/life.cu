@@ -164,7 +164,8 @@ struct RowBits {
 //   B3/S23: a live cell survives when S is 3 or 4; a dead cell is born when S is 3.
 // Only S mod 8 is formed (S0..S2): S = 8 and 9 read as 0 and 1, which neither rule distinguishes
 // from the true values (no birth, no survival either way).  Two full adders with 3-input logic
-// and one half adder: 7 operations for the count, 4 for the rule.
+// and one half adder: 7 operations for the count, 4 for the reference rule; B3/S23 folds birth
+// and survival into one mask (S in 3..4, and S != 4 for a dead cell).
 template <int RULE>
 __device__ __forceinline__ uint32_t life_combine(const RowBits& up, const RowBits& mid, const RowBits& dn, uint32_t o)
 {
@@ -174,14 +175,14 @@ __device__ __forceinline__ uint32_t life_combine(const RowBits& up, const RowBit
     const uint32_t y = (up.a1 & mid.a1) | (up.a1 & dn.a1) | (mid.a1 & dn.a1);
     const uint32_t s1 = x ^ c1, z = x & c1;
     const uint32_t s2 = y ^ z;
-    const uint32_t eq3 = ~s2 & s1 & s0;
     const uint32_t c = mid.w;
     if (RULE == APPFIS_GB_LIFE_REFERENCE) {
+        const uint32_t eq3 = ~s2 & s1 & s0;
         const uint32_t in345 = eq3 | (s2 & ~s1);
         return (c & in345 & o) | (~c & (eq3 | o));
     } else {
-        const uint32_t in34 = eq3 | (s2 & ~s1 & ~s0);
-        return (c & in34) | (~c & eq3);
+        const uint32_t in34 = (~s2 & s1 & s0) | (s2 & ~s1 & ~s0);
+        return in34 & (c | ~s2);
     }
 }
 struct RawBits {
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(256) life_bits_sweep(const uint32_t* __restric
 // generation writes the new state in place over the t-1 plane (new(x) reads only old(x) and
 // the current plane), then the planes swap.  The launch reads two planes and writes two planes
 // (the next launch needs both), so global traffic per generation drops by ~TB_STEPS/1.5.
-constexpr int TB_ROWS = 128;  // output rows per tile
+constexpr int TB_ROWS = 256;  // output rows per tile (72 KB of dynamic shared memory, 3 CTAs per SM)
 constexpr int TB_STEPS = 16;  // generations per launch (max)
 constexpr int TB_WARPS = 8;
 constexpr int TB_RR = TB_ROWS + 2 * TB_STEPS;
@@ -285,8 +286,9 @@ __global__ void __launch_bounds__(TB_WARPS * 32) life_bits_tb(const uint32_t* __
                                                                uint32_t* __restrict__ outCur, uint32_t* __restrict__ outOld,
                                                                int nw, int ny, int tiles_x, int tiles, int steps)
 {
-    __shared__ uint32_t sA[TB_RR][32];
-    __shared__ uint32_t sB[TB_RR][32];
+    extern __shared__ uint32_t tbsm[];  // two (TB_RR x 32)-word planes
+    uint32_t(*sA)[32] = reinterpret_cast<uint32_t(*)[32]>(tbsm);
+    uint32_t(*sB)[32] = reinterpret_cast<uint32_t(*)[32]>(tbsm + TB_RR * 32);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const int tx = tile % tiles_x, ty = tile / tiles_x;
@@ -311,6 +313,7 @@ __global__ void __launch_bounds__(TB_WARPS * 32) life_bits_tb(const uint32_t* __
             if (r0 < r1) {
                 RowBits up = tile_row(cur[r0 - 1][lane]);
                 RowBits mid = tile_row(cur[r0][lane]);
+#pragma unroll 4  // 4 rows per trip: the up/mid/dn rotation becomes register renaming
                 for (int r = r0; r < r1; r++) {
                     const RowBits dn = tile_row(cur[r + 1][lane]);
                     const uint32_t o = RULE == APPFIS_GB_LIFE_REFERENCE ? old[r][lane] : 0u;
@@ -450,14 +453,16 @@ int run_bits(uint32_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStr
         uint32_t* P[2][2] = {{buf[0], buf[1]}, {(uint32_t*)wc, (uint32_t*)wd}};  // [pair][cur/old]
         const int tiles_x = (nw + 29) / 30, tiles = tiles_x * ((ny + TB_ROWS - 1) / TB_ROWS);
         int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, life_bits_tb<RULE>, TB_WARPS * 32, 0) != cudaSuccess ||
+        const int tsm = 2 * TB_RR * 32 * 4;
+        GB_CUDA(cudaFuncSetAttribute(life_bits_tb<RULE>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm));
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, life_bits_tb<RULE>, TB_WARPS * 32, tsm) != cudaSuccess ||
             per_sm < 1)
             per_sm = 4;
         const int grid = std::max(1, std::min(tiles, per_sm * gb::sm_count()));
         int pair = 0;
         int done = 0;
         for (; done + TB_STEPS <= gens; done += TB_STEPS) {
-            life_bits_tb<RULE><<<grid, TB_WARPS * 32, 0, st>>>(P[pair][0], P[pair][1], P[1 - pair][0], P[1 - pair][1], nw, ny,
+            life_bits_tb<RULE><<<grid, TB_WARPS * 32, tsm, st>>>(P[pair][0], P[pair][1], P[1 - pair][0], P[1 - pair][1], nw, ny,
                                                                tiles_x, tiles, TB_STEPS);
             pair = 1 - pair;
         }
