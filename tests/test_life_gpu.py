@@ -67,7 +67,11 @@ def test_u8_vs_oracle(gb, torch_cuda, nx, ny, gens, rule):
         assert np.array_equal(cur, O.gol_b3s23(cells, gens))
 
 
-@pytest.mark.parametrize("nx,ny,gens", [(32, 1, 3), (32, 7, 5), (64, 40, 11), (1056, 66, 9), (2048, 130, 8), (96, 257, 21)])
+# 16+ generations run the time-blocked kernel: 30-word tile columns (1056 = 33 words: a second
+# column of 3 words; 960 = exactly one column; 32 = one word, fewer rows than the row halo),
+# partial last row tiles, and 2-3 launches plus a remainder.
+@pytest.mark.parametrize("nx,ny,gens", [(32, 1, 3), (32, 7, 5), (64, 40, 11), (1056, 66, 9), (2048, 130, 8), (96, 257, 21),
+                                        (1056, 300, 33), (960, 70, 16), (32, 20, 16), (2048, 700, 48), (160, 1100, 17)])
 @pytest.mark.parametrize("rule", [0, 1])
 def test_bits_vs_oracle(gb, torch_cuda, nx, ny, gens, rule):
     cells = W.gol_cells(nx, ny, 0.3, nx + 3 * ny)
@@ -105,18 +109,36 @@ def test_job_host_buffers(gb, torch_cuda, form):
 
 
 def test_full_size_forms_agree(gb, torch_cuda):
-    """16384^2 (the benchmark grid), 20 generations: the u8 and bit-packed forms give identical
-    states, the population matches a host count, and 10+10 generations equal 20 (restart)."""
+    """16384^2 (the benchmark grid), 36 generations (two time-blocked launches of 16, then 4
+    single sweeps): the u8 and bit-packed forms give identical states, the population matches a
+    host count, and 18+18 generations equal 36 (restart)."""
     nx = ny = 16384
     cells = W.gol_cells(nx, ny, 0.3, 42)
     a8 = np.zeros_like(cells)
     ab = np.zeros_like(cells)
     p8 = ctypes.c_int64(-1)
     pb = ctypes.c_int64(-2)
-    gb.call("appfis_gb_life_job", cells.ctypes.data, a8.ctypes.data, nx, ny, 20, 0, 0, ctypes.byref(p8))
-    gb.call("appfis_gb_life_job", cells.ctypes.data, ab.ctypes.data, nx, ny, 20, 0, 1, ctypes.byref(pb))
+    gb.call("appfis_gb_life_job", cells.ctypes.data, a8.ctypes.data, nx, ny, 36, 0, 0, ctypes.byref(p8))
+    gb.call("appfis_gb_life_job", cells.ctypes.data, ab.ctypes.data, nx, ny, 36, 0, 1, ctypes.byref(pb))
     assert np.array_equal(a8, ab)
     assert p8.value == pb.value == int(a8.sum(dtype=np.int64))
-    cur, prev = run_u8(gb, torch_cuda, cells, 10)
-    cur2, _ = run_u8(gb, torch_cuda, cur, 10, old=prev)
+    cur, prev = run_u8(gb, torch_cuda, cells, 18)
+    cur2, _ = run_u8(gb, torch_cuda, cur, 18, old=prev)
     assert np.array_equal(cur2, a8)
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+def test_large_ragged_columns_forms_agree(gb, torch_cuda, rule):
+    """15904 x 12000 (497 words: 16 full 30-word columns and one of 17 words; 47 row tiles, the
+    last of 224 rows), 32 generations: bit-packed and u8 forms agree (the u8 form is pinned to
+    the oracle above)."""
+    nx, ny = 15904, 12000
+    cells = W.gol_cells(nx, ny, 0.3, 9)
+    a8 = np.zeros_like(cells)
+    ab = np.zeros_like(cells)
+    p8 = ctypes.c_int64(-1)
+    pb = ctypes.c_int64(-2)
+    gb.call("appfis_gb_life_job", cells.ctypes.data, a8.ctypes.data, nx, ny, 32, rule, 0, ctypes.byref(p8))
+    gb.call("appfis_gb_life_job", cells.ctypes.data, ab.ctypes.data, nx, ny, 32, rule, 1, ctypes.byref(pb))
+    assert np.array_equal(a8, ab)
+    assert p8.value == pb.value
