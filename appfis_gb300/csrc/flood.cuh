@@ -38,6 +38,7 @@ struct Ctl {
 
 struct Params {
     double dx, cn, hextra, t_end, print_interval, time_step;
+    float fdx, fcn, fhextra;  // dx, cn, hextra rounded to float once on the host (float kernel)
     int max_steps, ndom;
     long long total_strips;
     double* dtlog;  // [ndom][max_steps] or null
@@ -87,6 +88,17 @@ __device__ __forceinline__ int find_domain(const Dom<T>* d, int nd, long long s)
     return lo;
 }
 
+// A parameter in the kernel's type: the float kernel takes the host-rounded copy (the same value
+// as converting on the device, without a double-to-float conversion on the FP64 pipe per strip).
+template <class T>
+__device__ __forceinline__ T typed(double d, float f)
+{
+    if constexpr (sizeof(T) == 4)
+        return f;
+    else
+        return d;
+}
+
 __device__ __forceinline__ double step_dt(const Ctl* ctl, int cur, int d, const Params& p, double big)
 {
     double dt = __longlong_as_double((long long)ctl->dtbits[cur][d]);
@@ -122,8 +134,8 @@ __device__ void phase_a(const Dom<T> D, Ctl* ctl, int cur, int d, long long loca
     T* __restrict__ qy = D.qy[b];
     const T* __restrict__ dem = D.dem;
     const int px = D.px;
-    const T hextra = (T)p.hextra, E = K<T>::dry(), G = K<T>::g();
-    const T dx = (T)p.dx, cn = (T)p.cn;
+    const T hextra = typed<T>(p.hextra, p.fhextra), E = K<T>::dry(), G = K<T>::g();
+    const T dx = typed<T>(p.dx, p.fdx), cn = typed<T>(p.cn, p.fcn);
     T mn = K<T>::big();  // min in T (exact), widened once per warp: no per-cell FP64 work in float
     if (lane >= 1 && lane <= SCOLS && i <= D.nx) {
         for (int jb = j0; jb < j1; jb += FA_ROWS) {
@@ -209,7 +221,7 @@ __device__ bool phase_b(const Dom<T> D, long long local, int b, T dt, const Para
     const int j0 = 1 + sy * ROWS, j1 = min(j0 + ROWS, D.ny + 1);
     const bool own = lane >= 1 && lane <= SCOLS && i <= D.nx;  // cells this lane updates
     const bool xface = lane <= SCOLS && i <= D.nx;             // face i|i+1 is needed
-    const T dx = (T)p.dx, hextra = (T)p.hextra;
+    const T dx = typed<T>(p.dx, p.fdx), hextra = typed<T>(p.hextra, p.fhextra);
     const T one = T(1), zero = T(0);
     const T* __restrict__ h = D.h[b];
     const T* __restrict__ qx = D.qx[b];

@@ -129,6 +129,9 @@ int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_para
     p.dx = prm->dx;
     p.cn = prm->courant;
     p.hextra = prm->hextra;
+    p.fdx = (float)prm->dx;
+    p.fcn = (float)prm->courant;
+    p.fhextra = (float)prm->hextra;
     p.t_end = prm->t_end;
     p.print_interval = prm->print_interval;
     p.time_step = prm->time_step;
