@@ -1,7 +1,10 @@
 // Packed FP32 pair arithmetic (add/sub/mul/fma .rn.f32x2, sm_100 family): one instruction does
 // the same round-to-nearest operation on two lanes, halving the FP32 instruction count of a
-// kernel that updates two points per thread.  Each lane's result is what the scalar instruction
-// gives, so lane-wise expressions keep their rounding; only the pairing is new.
+// kernel that updates two points per thread.  The code generator contracts a pair multiply that
+// feeds a pair add into one pair FMA (measured on sm_103a, with or without -fmad=false, even
+// when the multiply is written as an FMA with a -0 addend), so a chain of them rounds like the
+// FMA form: kernels that must round exactly like separate scalar operations use the scalar
+// __fmul_rn / __fadd_rn intrinsics instead.
 #pragma once
 
 #include <cuda_fp16.h>

@@ -7,10 +7,10 @@
 // contraction), so every point is bit-identical to the reference's CPU path.
 //
 // The 1024^2 workload is 8.4 MB for both buffers, so it lives in L2; one launch per sweep would
-// be launch-bound.  heat2d_blocked therefore runs S sweeps per launch on a tile held in shared
-// memory (overlapped tiling: the tile plus an S-deep halo is loaded once, each sweep shrinks the
-// valid region by one cell, the centre tile is written back).  Ghost-ring cells are loaded and
-// held constant, so Dirichlet boundaries are exact for any S.
+// be launch-bound.  heat2d_regs therefore runs S sweeps per launch on a tile held on chip
+// (overlapped tiling: the tile plus an S-deep halo is loaded once, each sweep shrinks the valid
+// region by one cell, the centre tile is written back).  Ghost-ring cells are loaded and held
+// constant, so Dirichlet boundaries are exact for any S.
 #include "gb_common.cuh"
 
 namespace {
@@ -34,69 +34,117 @@ __global__ void __launch_bounds__(256) heat2d_sweep_k(const float* __restrict__ 
                         cx, cy);
 }
 
-// Overlapped tiling: output tile TX x TY, halo S (runtime, <= SMAX), S sweeps per launch.
-// Threads form a 32 x 8 grid that strides over the shared region (no index division).
-template <int TX, int TY, int SMAX>
-__global__ void __launch_bounds__(256) heat2d_blocked(const float* __restrict__ cur, float* __restrict__ nxt, int nx,
-                                                       int ny, int pitch, int S, float cx, float cy)
+// Overlapped tiling: output tile TX x TY, halo S (runtime, <= SMAX), S sweeps per launch.  The
+// (TX + 2 SMAX) x (TY + 2 SMAX) region is cut into 4 x 4 blocks, one per thread, held in
+// registers for all S sweeps.  A sweep publishes each block's four edges (top and bottom rows,
+// left and right columns, one 16-byte vector each) into shared memory, synchronises once, reads
+// the facing edges of the four neighbour blocks and updates its 16 points: 8 shared-memory
+// vector operations per 16 point-updates.  Ghost-ring cells and cells outside the field keep
+// their values; every other cell of the region is updated each sweep (those outside the
+// shrinking valid window only feed cells that are not written back).  The point update is
+// heat_point, scalar: packed FP32-pair multiplies feeding pair adds are contracted to pair FMAs
+// by the code generator, which would change the rounding.
+constexpr int RBS = 4;  // block side
+
+template <int BX, int BY>
+struct HeatEdges {  // block edges, by sweep parity
+    float4 t[2][BY][BX], b[2][BY][BX], l[2][BY][BX], r[2][BY][BX];
+};
+
+// One tile, S sweeps (unrolled: the sweep-to-sweep register copies become renaming).  MASK:
+// the region reaches the ghost ring or beyond the field, so loads are guarded and only interior
+// cells are updated; tiles whose whole region is interior take the unmasked form.
+template <int TX, int TY, int SMAX, int S, bool MASK>
+__device__ __forceinline__ void heat_tile(const float* __restrict__ cur, float* __restrict__ nxt, int nx, int ny, int pitch,
+                                          float cx, float cy, HeatEdges<(TX + 2 * SMAX) / RBS, (TY + 2 * SMAX) / RBS>& e)
 {
-    constexpr int RW = TX + 2 * SMAX, RH = TY + 2 * SMAX;  // shared region (max)
-    extern __shared__ float sm[];
-    float* A = sm;
-    float* B = sm + RW * RH;
-    const int rw = TX + 2 * S, rh = TY + 2 * S;  // region actually used
-    const int ox = 1 + blockIdx.x * TX - S;      // padded coords of region (0,0)
-    const int oy = 1 + blockIdx.y * TY - S;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-
-    // load the region: all loads of a thread are issued before any is stored (one L2 round trip)
-    constexpr int LR = (RH + 7) / 8, LC = (RW + 31) / 32;
-    float v[LR][LC];
+    constexpr int BX = (TX + 2 * SMAX) / RBS, BY = (TY + 2 * SMAX) / RBS;
+    constexpr int rw = TX + 2 * S, rh = TY + 2 * S;  // region in use
+    const int t = threadIdx.x, bx = t % BX, by = t / BX;
+    const int ox = 1 + blockIdx.x * TX - S, oy = 1 + blockIdx.y * TY - S;  // padded coords of region (0,0)
+    float v[RBS][RBS];
+    unsigned upd = 0;  // MASK: bit 4r+c set for an interior cell of the region in use
 #pragma unroll
-    for (int a = 0; a < LR; a++)
+    for (int r = 0; r < RBS; r++)
 #pragma unroll
-        for (int c = 0; c < LC; c++) {
-            const int ry = ty + 8 * a, rx = tx + 32 * c, gy = oy + ry, gx = ox + rx;
-            v[a][c] = (ry < rh && rx < rw && gx >= 0 && gx <= nx + 1 && gy >= 0 && gy <= ny + 1)
-                          ? __ldg(cur + (size_t)gy * pitch + gx) : 0.0f;
-        }
-#pragma unroll
-    for (int a = 0; a < LR; a++)
-#pragma unroll
-        for (int c = 0; c < LC; c++) {
-            const int ry = ty + 8 * a, rx = tx + 32 * c;
-            if (ry < rh && rx < rw) {
-                A[ry * RW + rx] = v[a][c];
-                B[ry * RW + rx] = v[a][c];  // ghost / outside cells keep their value in both buffers
+        for (int c = 0; c < RBS; c++) {
+            const int rx = RBS * bx + c, ry = RBS * by + r, gx = ox + rx, gy = oy + ry;
+            if (MASK) {
+                const bool used = rx < rw && ry < rh;
+                v[r][c] = (used && gx >= 0 && gx <= nx + 1 && gy >= 0 && gy <= ny + 1) ? __ldg(cur + (size_t)gy * pitch + gx) : 0.0f;
+                if (used && gx >= 1 && gx <= nx && gy >= 1 && gy <= ny) upd |= 1u << (RBS * r + c);
+            } else {
+                v[r][c] = __ldg(cur + (size_t)gy * pitch + gx);
             }
         }
-    __syncthreads();
-
-    // interior cells of the region (those updated by the sweep), in region coordinates
-    const int ix0 = max(1 - ox, 0), ix1 = min(nx + 1 - ox, rw);  // gx in [1, nx]
-    const int iy0 = max(1 - oy, 0), iy1 = min(ny + 1 - oy, rh);
+    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
     for (int s = 1; s <= S; s++) {
-        // valid after this sweep: region cells [s, rw-s) x [s, rh-s)
-        const int x0 = max(s, ix0), x1 = min(rw - s, ix1), y0 = max(s, iy0), y1 = min(rh - s, iy1);
-        for (int ry = y0 + ty; ry < y1; ry += 8)
-            for (int rx = x0 + tx; rx < x1; rx += 32) {
-                const int q = ry * RW + rx;
-                B[q] = heat_point(A[q], A[q - 1], A[q + 1], A[q - RW], A[q + RW], cx, cy);
-            }
+        // one barrier per sweep: a buffer is rewritten two sweeps later, after every thread has
+        // passed the next sweep's barrier and so finished reading it
+        const int q = s & 1;
+        e.t[q][by][bx] = make_float4(v[0][0], v[0][1], v[0][2], v[0][3]);
+        e.b[q][by][bx] = make_float4(v[3][0], v[3][1], v[3][2], v[3][3]);
+        e.l[q][by][bx] = make_float4(v[0][0], v[1][0], v[2][0], v[3][0]);
+        e.r[q][by][bx] = make_float4(v[0][3], v[1][3], v[2][3], v[3][3]);
         __syncthreads();
-        float* t = A;
-        A = B;
-        B = t;
+        const float4 up = by > 0 ? e.b[q][by - 1][bx] : z4;
+        const float4 dn = by < BY - 1 ? e.t[q][by + 1][bx] : z4;
+        const float4 lf = bx > 0 ? e.r[q][by][bx - 1] : z4;
+        const float4 rt = bx < BX - 1 ? e.l[q][by][bx + 1] : z4;
+        const float upv[RBS] = {up.x, up.y, up.z, up.w}, dnv[RBS] = {dn.x, dn.y, dn.z, dn.w};
+        const float lfv[RBS] = {lf.x, lf.y, lf.z, lf.w}, rtv[RBS] = {rt.x, rt.y, rt.z, rt.w};
+        float nv[RBS][RBS];
+#pragma unroll
+        for (int r = 0; r < RBS; r++)
+#pragma unroll
+            for (int c = 0; c < RBS; c++) {
+                const float l = c > 0 ? v[r][c - 1] : lfv[r], rr = c + 1 < RBS ? v[r][c + 1] : rtv[r];
+                const float u = r > 0 ? v[r - 1][c] : upv[c], d = r + 1 < RBS ? v[r + 1][c] : dnv[c];
+                const float h = heat_point(v[r][c], l, rr, u, d, cx, cy);
+                nv[r][c] = !MASK || ((upd >> (RBS * r + c)) & 1u) ? h : v[r][c];
+            }
+#pragma unroll
+        for (int r = 0; r < RBS; r++)
+#pragma unroll
+            for (int c = 0; c < RBS; c++) v[r][c] = nv[r][c];
     }
-
-    for (int y = ty; y < TY; y += 8) {
-        const int gy = 1 + blockIdx.y * TY + y;
-        if (gy > ny) break;
-        for (int x = tx; x < TX; x += 32) {
-            const int gx = 1 + blockIdx.x * TX + x;
-            if (gx <= nx) nxt[(size_t)gy * pitch + gx] = A[(y + S) * RW + (x + S)];
+#pragma unroll
+    for (int r = 0; r < RBS; r++)
+#pragma unroll
+        for (int c = 0; c < RBS; c++) {
+            const int x = RBS * bx + c - S, y = RBS * by + r - S;  // output tile coordinates
+            const int gx = 1 + blockIdx.x * TX + x, gy = 1 + blockIdx.y * TY + y;
+            if (x >= 0 && x < TX && y >= 0 && y < TY && (!MASK || (gx <= nx && gy <= ny))) nxt[(size_t)gy * pitch + gx] = v[r][c];
         }
+}
+
+template <int TX, int TY, int SMAX, int S>
+__global__ void __launch_bounds__(((TX + 2 * SMAX) / RBS) * ((TY + 2 * SMAX) / RBS))
+    heat2d_regs(const float* __restrict__ cur, float* __restrict__ nxt, int nx, int ny, int pitch, float cx, float cy)
+{
+    constexpr int BX = (TX + 2 * SMAX) / RBS, BY = (TY + 2 * SMAX) / RBS;
+    static_assert(BX * RBS == TX + 2 * SMAX && BY * RBS == TY + 2 * SMAX, "region in whole blocks");
+    static_assert(S >= 1 && S <= SMAX, "sweeps per launch");
+    __shared__ HeatEdges<BX, BY> e;
+    // the whole region (TX + 2 SMAX wide, loaded in full) lies on interior cells
+    const bool inner = S == SMAX && (int)blockIdx.x * TX >= S && (int)blockIdx.y * TY >= S &&
+                       ((int)blockIdx.x + 1) * TX + S <= nx && ((int)blockIdx.y + 1) * TY + S <= ny;
+    if (inner)
+        heat_tile<TX, TY, SMAX, S, false>(cur, nxt, nx, ny, pitch, cx, cy, e);
+    else
+        heat_tile<TX, TY, SMAX, S, true>(cur, nxt, nx, ny, pitch, cx, cy, e);
+}
+
+template <int TX, int TY, int SMAX, int S = SMAX>
+void launch_heat_regs(int s, dim3 grd, const float* cur, float* nxt, int nx, int ny, int pitch, float cx, float cy,
+                      cudaStream_t st)
+{
+    if constexpr (S > 1) {
+        if (s < S) return launch_heat_regs<TX, TY, SMAX, S - 1>(s, grd, cur, nxt, nx, ny, pitch, cx, cy, st);
     }
+    constexpr int threads = ((TX + 2 * SMAX) / RBS) * ((TY + 2 * SMAX) / RBS);
+    heat2d_regs<TX, TY, SMAX, S><<<grd, threads, 0, st>>>(cur, nxt, nx, ny, pitch, cx, cy);
 }
 
 constexpr int HTX = 64, HTY = 32, HSMAX = 8;
@@ -126,18 +174,16 @@ int appfis_gb_heat2d(float* a, float* b, int nx, int ny, int pitch, int iters, f
     GB_TRY(check_heat(a, b, nx, ny, pitch));
     if (iters < 0) return gb::fail(APPFIS_GB_EINVAL, "heat2d: negative iteration count");
     cudaStream_t st = gb::as_stream(stream);
-    constexpr size_t smem = sizeof(float) * 2 * (HTX + 2 * HSMAX) * (HTY + 2 * HSMAX);
-    GB_CUDA(cudaFuncSetAttribute(heat2d_blocked<HTX, HTY, HSMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grd(gb::ceil_div(nx, HTX), gb::ceil_div(ny, HTY));
     float* buf[2] = {a, b};
     int ci = 0;
     for (int done = 0; done < iters;) {
         const int S = std::min(HSMAX, iters - done);
-        heat2d_blocked<HTX, HTY, HSMAX><<<grd, 256, smem, st>>>(buf[ci], buf[1 - ci], nx, ny, pitch, S, cx, cy);
+        launch_heat_regs<HTX, HTY, HSMAX>(S, grd, buf[ci], buf[1 - ci], nx, ny, pitch, cx, cy, st);
         ci = 1 - ci;
         done += S;
     }
-    GB_TRY(gb::launched("heat2d_blocked"));
+    GB_TRY(gb::launched("heat2d_regs"));
     if (cur_index) *cur_index = ci;
     return APPFIS_GB_OK;
 }

@@ -524,8 +524,8 @@ def bench_heat(torch, gb, W, dev, sp, hbm):
     gbs = lups * 8 / (best * 1e-3) / 1e9
     return {"workload": "heat2d 1024^2 FP32, 1000 iterations, Dirichlet", "glups": lups / (best * 1e-3) / 1e9, "ms": best,
             "ms_stream_launches": ms, "ms_cuda_graph": ms_g, "bytes_per_lup": 8, "effective_gbs": gbs, "frac_of_hbm": gbs / hbm,
-            "note": "8.4 MB working set is L2-resident; 8 sweeps per launch in shared memory (125 launches, replayed "
-                    "from a CUDA graph); HBM fraction is nominal",
+            "note": "8.4 MB working set is L2-resident; 8 sweeps per launch on chip (4x4 point blocks in registers, "
+                    "block edges through shared memory; 125 launches, replayed from a CUDA graph); HBM fraction is nominal",
             "form": "plain FP32 (bit-identical to the reference CPU path)"}
 
 
@@ -767,7 +767,7 @@ def profile_case(name, local):
     himeno: 257x257x513 (rows padded to 264), 5 plain sweeps (himeno_tma<0>), 5 mixed sweeps
             (himeno_tma<1>, himeno_correct)
     fdtd:   512^3, 5 FP32 steps then 5 FP16 steps (star_r4_tma)
-    heat:   1024^2, 16 iterations (2 heat2d_blocked launches)
+    heat:   1024^2, 16 iterations (2 heat2d_regs launches)
     flood:  the 32-domain batch (80 M cells, ~2.6 GB), 20 steps (one flood_persistent launch)"""
     import torch
 
