@@ -3,7 +3,9 @@
 // for the per-face / per-cell arithmetic and the reference it follows.
 //
 // One cooperative launch advances a batch of independent domains of uneven sizes to t_end.
-// Work items are strips (32 columns x ROWS rows) of all domains, visited grid-stride by warps.
+// Work items are strips (SCOLS interior columns x ROWS rows) of all domains; in each phase warps
+// take them one at a time from a counter (a strip's cost follows the water, so a fixed stride
+// leaves some warps with far more wet strips than others).
 // Each step is phase A (wet/dry fix of the previous step + CFL dt, min per domain) and phase B
 // (fluxes + update into the other state buffer), separated by grid barriers whose spin waits
 // are bounded (on timeout the kernel records an error and returns).  Per-domain scalars
@@ -34,6 +36,8 @@ struct Ctl {
     unsigned bar_count;
     unsigned bar_gen;
     int error;
+    unsigned ticket[2];  // phase A strip hand-out, by step parity
+    unsigned ticketb[2];  // phase B strip hand-out, by step parity
 };
 
 struct Params {
@@ -315,6 +319,24 @@ struct DomCtl {
     unsigned char flags[MAXD];  // bit 0: state buffer b, bit 1: fix, bit 2: wants dt / runs phase B
 };
 
+// Strips of one phase: warp w first takes strip w, then strips nwarps + k for the tickets k it
+// draws from *ctr (zeroed after the phase's grid barrier, for its next use two steps later).
+// The next ticket is requested before the current strip is processed, so its latency hides
+// behind the work.  Warps without a first strip draw none (a batch smaller than the grid costs
+// no atomics).
+template <class F>
+__device__ __forceinline__ void for_strips(unsigned* ctr, long long first, long long nwarps, long long total, int lane, F&& body)
+{
+    long long s = first;
+    unsigned tk = 0;
+    if (s < total && lane == 0) tk = atomicAdd(ctr, 1u);
+    while (s < total) {
+        body(s);
+        s = nwarps + (long long)__shfl_sync(0xffffffffu, tk, 0);
+        if (s < total && lane == 0) tk = atomicAdd(ctr, 1u);
+    }
+}
+
 // CTAs per SM the FP32 kernel's register allocation targets (FP64: 1).
 #ifndef FLOOD_F32_MIN_BLOCKS
 #define FLOOD_F32_MIN_BLOCKS 3
@@ -345,13 +367,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
             dc.flags[d] = (unsigned char)((ctl->steps[cur][d] & 1) | (fix ? 2 : 0) | (want ? 4 : 0));
         }
         __syncthreads();
-        for (long long s = warp; s < p.total_strips; s += nwarps) {
+        for_strips(&ctl->ticket[cur], warp, nwarps, p.total_strips, lane, [&](long long s) {
             const int d = find_domain(doms, p.ndom, s);
             const int f = dc.flags[d];
-            if (SKIP && p.zc[(size_t)cur * p.total_strips + s] >= 1) continue;  // dry input: no fix, no dt
+            if (SKIP && p.zc[(size_t)cur * p.total_strips + s] >= 1) return;  // dry input: no fix, no dt
             if (f & 6) phase_a<T>(doms[d], ctl, cur, d, s - doms[d].strip0, f & 1, (f & 2) != 0, (f & 4) != 0, p);
-        }
+        });
         if (!grid_barrier(ctl)) return;
+        if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ticket[cur] = 0;  // next used two steps later, past a barrier
         int active = 0;
         if (threadIdx.x < p.ndom) {
             const int d = threadIdx.x;
@@ -371,7 +394,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
             return;
         }
         // phase B
-        for (long long s = warp; s < p.total_strips; s += nwarps) {
+        for_strips(&ctl->ticketb[cur], warp, nwarps, p.total_strips, lane, [&](long long s) {
             const int d = find_domain(doms, p.ndom, s);
             const int f = dc.flags[d];
             if (SKIP) {
@@ -380,14 +403,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
                 const unsigned char z = zin[s];
                 if (!(f & 4) || strip_idle(doms[d], zin, s)) {  // unchanged state
                     if (lane == 0) zout[s] = z;
-                    continue;
+                    return;
                 }
                 const bool dry = phase_b<T>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p);
                 if (lane == 0) zout[s] = dry ? (unsigned char)(z < 2 ? z + 1 : 2) : 0;
             } else if (f & 4) {
                 phase_b<T>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p);
             }
-        }
+        });
         if (blockIdx.x == 0 && threadIdx.x == 0) {  // commit the per-domain scalars of step n
             for (int d = 0; d < p.ndom; d++) {
                 if (is_active(ctl, cur, d, p)) {
@@ -410,6 +433,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
             }
         }
         if (!grid_barrier(ctl)) return;
+        if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ticketb[cur] = 0;  // next used two steps later, past a barrier
     }
 }
 
@@ -420,6 +444,8 @@ static __global__ void flood_init_ctl(Ctl* ctl, int ndom, double big, double t0)
         ctl->bar_count = 0;
         ctl->bar_gen = 0;
         ctl->error = 0;
+        ctl->ticket[0] = ctl->ticket[1] = 0;
+        ctl->ticketb[0] = ctl->ticketb[1] = 0;
     }
     if (d < ndom) {
         for (int k = 0; k < 2; k++) {
