@@ -92,21 +92,39 @@ namespace APPFIS
 			if (i < x1) STENCIL(i, Holder<A>(args).get()...);
 		}
 
+		// Rows (2-D) or planes (3-D) per thread: a thread calls the functor for MARCH consecutive
+		// points along its slowest axis, so the neighbour values of one call are in L1 for the next.
+		// Every point of the box is still visited exactly once, in no particular order.  In 3-D the
+		// march pays only for functors over a few fields (measured on GB300: the radius-4 star over
+		// 2 arrays 107 -> 139 GLUP/s; Himeno over 14 arrays 68 -> 48, its loads in flight are what
+		// count), so functors taking more than MARCH_MAX_ARRAYS arrays keep one point per thread.
+		constexpr int MARCH = 4, MARCH_MAX_ARRAYS = 4;
+
+		template<class A> struct IsArrayArg { static const int value = 0; };
+		template<class U> struct IsArrayArg<ArrayArg<U> > { static const int value = 1; };
+		template<class... A> struct ArrayCount { static const int value = 0; };
+		template<class H, class... R> struct ArrayCount<H, R...>
+		{
+			static const int value = IsArrayArg<H>::value + ArrayCount<R...>::value;
+		};
+
 		template<class... A>
 		__global__ void Functor2D(int x0, int x1, int y0, int y1, A... args)
 		{
 			const int i = x0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-			const int j = y0 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-			if (i < x1 && j < y1) STENCIL(i, j, Holder<A>(args).get()...);
+			const int jb = y0 + (int)(blockIdx.y * blockDim.y + threadIdx.y) * MARCH;
+			if (i >= x1) return;
+			for (int j = jb; j < jb + MARCH && j < y1; j++) STENCIL(i, j, Holder<A>(args).get()...);
 		}
 
-		template<class... A>
+		template<int M, class... A>
 		__global__ void Functor3D(int x0, int x1, int y0, int y1, int z0, int z1, A... args)
 		{
 			const int i = x0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
 			const int j = y0 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-			const int k = z0 + (int)(blockIdx.z * blockDim.z + threadIdx.z);
-			if (i < x1 && j < y1 && k < z1) STENCIL(i, j, k, Holder<A>(args).get()...);
+			const int kb = z0 + (int)(blockIdx.z * blockDim.z + threadIdx.z) * M;
+			if (i >= x1 || j >= y1) return;
+			for (int k = kb; k < kb + M && k < z1; k++) STENCIL(i, j, k, Holder<A>(args).get()...);
 		}
 
 		inline unsigned Blocks(int n, int b) { return (unsigned)((n + b - 1) / b); }
@@ -185,7 +203,7 @@ namespace APPFIS
 		const int x0 = config.GetStartX(), x1 = config.GetEndX(), y0 = config.GetStartY(), y1 = config.GetEndY();
 		if (x1 > x0 && y1 > y0)
 		{
-			dim3 blk(32, 8), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 8));
+			dim3 blk(32, 8), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 8 * detail::MARCH));
 			detail::Functor2D<typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
 				x0, x1, y0, y1, detail::KArg<TArgs>::to(args)...);
 		}
@@ -199,9 +217,18 @@ namespace APPFIS
 		const int z0 = config.GetStartZ(), z1 = config.GetEndZ();
 		if (x1 > x0 && y1 > y0 && z1 > z0)
 		{
-			dim3 blk(32, 4, 2), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 4), detail::Blocks(z1 - z0, 2));
-			detail::Functor3D<typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
-				x0, x1, y0, y1, z0, z1, detail::KArg<TArgs>::to(args)...);
+			if (detail::ArrayCount<typename detail::KArg<TArgs>::type...>::value <= detail::MARCH_MAX_ARRAYS)
+			{
+				dim3 blk(32, 8, 1), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 8), detail::Blocks(z1 - z0, detail::MARCH));
+				detail::Functor3D<detail::MARCH, typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
+					x0, x1, y0, y1, z0, z1, detail::KArg<TArgs>::to(args)...);
+			}
+			else
+			{
+				dim3 blk(32, 4, 2), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 4), detail::Blocks(z1 - z0, 2));
+				detail::Functor3D<1, typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
+					x0, x1, y0, y1, z0, z1, detail::KArg<TArgs>::to(args)...);
+			}
 		}
 		detail::AfterSweep(config);
 	}
