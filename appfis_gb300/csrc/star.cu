@@ -313,7 +313,9 @@ __global__ void __launch_bounds__(256) star_r4_vec(const T* __restrict__ in, T* 
 // slot's mbarrier.  Thread 0 keeps TNS - 5 planes in flight beyond the newest one in use.  Each
 // thread pushes its centre values of plane k+4 into its z queue (registers); the x/y windows of
 // plane k come from the ring, except the thread's own rows, which are the queue's centre
-// entries.  The arithmetic runs on x pairs with packed FP32-pair instructions.  VXT = 4 reads
+// entries.  The arithmetic runs on x pairs with packed FP32-pair instructions, except the x sums
+// at odd shifts: their operand pairs straddle register pairs, and two scalar adds cost less than
+// assembling the pairs (the same round-to-nearest additions either way).  VXT = 4 reads
 // 16-byte shared vectors (fewer shared-memory wavefronts); VXT = 2 halves the queue registers
 // (twice the resident warps).  Global traffic: each plane read once per CTA (plus the 8-plane
 // z-chunk overlap), each result written once.
@@ -480,8 +482,10 @@ __global__ void __launch_bounds__(128, VXT == 4 ? 4 : 6) star_r4_tma(const __gri
                             v = cen;
 #pragma unroll
                             for (int a = 1; a <= R; a++) {
-                                const float2 sx = f2::add(make_float2(xw[R + c - a], xw[R + c + 1 - a]),
-                                                          make_float2(xw[R + c + a], xw[R + c + 1 + a]));
+                                const float2 sx = (a & 1) ? make_float2(__fadd_rn(xw[R + c - a], xw[R + c + a]),
+                                                                        __fadd_rn(xw[R + c + 1 - a], xw[R + c + 1 + a]))
+                                                          : f2::add(make_float2(xw[R + c - a], xw[R + c + 1 - a]),
+                                                                    make_float2(xw[R + c + a], xw[R + c + 1 + a]));
                                 const float2 sy = f2::add(make_float2(ym[a - 1]->v[c], ym[a - 1]->v[c + 1]),
                                                           make_float2(yp[a - 1]->v[c], yp[a - 1]->v[c + 1]));
                                 const VecN<VXT>& zm = q[r][(P + 4 - a) % 9];
@@ -494,8 +498,10 @@ __global__ void __launch_bounds__(128, VXT == 4 ? 4 : 6) star_r4_tma(const __gri
                             v = f2::mul(f2::splat(wt.w[0]), cen);
 #pragma unroll
                             for (int a = 1; a <= R; a++) {
-                                const float2 sx = f2::add(make_float2(xw[R + c - a], xw[R + c + 1 - a]),
-                                                          make_float2(xw[R + c + a], xw[R + c + 1 + a]));
+                                const float2 sx = (a & 1) ? make_float2(__fadd_rn(xw[R + c - a], xw[R + c + a]),
+                                                                        __fadd_rn(xw[R + c + 1 - a], xw[R + c + 1 + a]))
+                                                          : f2::add(make_float2(xw[R + c - a], xw[R + c + 1 - a]),
+                                                                    make_float2(xw[R + c + a], xw[R + c + 1 + a]));
                                 const float2 sy = f2::add(make_float2(ym[a - 1]->v[c], ym[a - 1]->v[c + 1]),
                                                           make_float2(yp[a - 1]->v[c], yp[a - 1]->v[c + 1]));
                                 const VecN<VXT>& zm = q[r][(P + 4 - a) % 9];
