@@ -532,14 +532,20 @@ __global__ void __launch_bounds__(MX / 2 * MY) himeno_mixed2(const __grid_consta
             for (int n = 0; n < 10; n++) co[n] = __half22float2(reinterpret_cast<const __half2*>(st + n * MX * MY * 2)[cq / 2]);
             const float2 a3 = reinterpret_cast<const float2*>(st + 10 * MX * MY * 2)[cq / 2];
             const float2 D = __half22float2(reinterpret_cast<const __half2*>(st + 10 * MX * MY * 2 + MX * MY * 4)[cq / 2]);
-            // a0 a1 a2 b0 b1 b2 c0 c1 c2 bnd
-            float2 ne = f2::mul(co[0], xp);
+            // a0 a1 a2 b0 b1 b2 c0 c1 c2 bnd.  Terms with x neighbours take one value from the
+            // next pair over, so their operands straddle register pairs: those are formed lane by
+            // lane with scalar round-to-nearest operations (the same per-lane arithmetic).
+            float2 ne = make_float2(__fmul_rn(co[0].x, xp.x), __fmul_rn(co[0].y, xp.y));
             ne = f2::fma(co[1], yp, ne);
             ne = f2::fma(co[2], zp, ne);
-            ne = f2::fma(co[3], f2::sub(f2::sub(xpyp, xpym), f2::sub(xmyp, xmym)), ne);
+            const float2 txy = make_float2(__fsub_rn(__fsub_rn(xpyp.x, xpym.x), __fsub_rn(xmyp.x, xmym.x)),
+                                           __fsub_rn(__fsub_rn(xpyp.y, xpym.y), __fsub_rn(xmyp.y, xmym.y)));
+            ne = f2::fma(co[3], txy, ne);
             ne = f2::fma(co[4], f2::sub(f2::sub(ypzp, ymzp), f2::sub(ypzm, ymzm)), ne);
-            ne = f2::fma(co[5], f2::sub(f2::sub(xpzp, xmzp), f2::sub(xpzm, xmzm)), ne);
-            ne = f2::fma(co[6], xm, ne);
+            const float2 txz = make_float2(__fsub_rn(__fsub_rn(xpzp.x, xmzp.x), __fsub_rn(xpzm.x, xmzm.x)),
+                                           __fsub_rn(__fsub_rn(xpzp.y, xmzp.y), __fsub_rn(xpzm.y, xmzm.y)));
+            ne = f2::fma(co[5], txz, ne);
+            ne = make_float2(__fmaf_rn(co[6].x, xm.x, ne.x), __fmaf_rn(co[6].y, xm.y, ne.y));
             ne = f2::fma(co[7], ym, ne);
             ne = f2::fma(co[8], zm, ne);
             const float2 v = f2::add(f2::fma(f2::mul(wsplat, co[9]), f2::sub(f2::mul(a3, ne), e0), e0), D);
