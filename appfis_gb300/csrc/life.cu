@@ -163,26 +163,37 @@ struct RowBits {
 //     otherwise; a dead cell is born when S is 3 and otherwise keeps o;
 //   B3/S23: a live cell survives when S is 3 or 4; a dead cell is born when S is 3.
 // Only S mod 8 is formed (S0..S2): S = 8 and 9 read as 0 and 1, which neither rule distinguishes
-// from the true values (no birth, no survival either way).  Two full adders with 3-input logic
-// and one half adder: 7 operations for the count, 4 for the reference rule; B3/S23 folds birth
-// and survival into one mask (S in 3..4, and S != 4 for a dead cell).
+// from the true values (no birth, no survival either way).  Every step is one explicit 3-input
+// logic instruction (lop3): 6 for the count (two full adders and the half adder folded into
+// s2 = y ^ (x & c1)), 3 for the reference rule (the window S in 3..5, narrowed to S == 3 for a
+// dead cell, then the keep/birth select with the stale value) and 2 for B3/S23.
+// One 3-input logic instruction; LUT = f(0xF0, 0xCC, 0xAA) for the function f(a, b, c).
+template <unsigned LUT>
+__device__ __forceinline__ uint32_t lop3(uint32_t a, uint32_t b, uint32_t c)
+{
+    uint32_t d;
+    asm("lop3.b32 %0, %1, %2, %3, %4;" : "=r"(d) : "r"(a), "r"(b), "r"(c), "n"(LUT));
+    return d;
+}
+constexpr unsigned XOR3 = 0x96, MAJ3 = 0xE8;
+
 template <int RULE>
 __device__ __forceinline__ uint32_t life_combine(const RowBits& up, const RowBits& mid, const RowBits& dn, uint32_t o)
 {
-    const uint32_t s0 = up.a0 ^ mid.a0 ^ dn.a0;
-    const uint32_t c1 = (up.a0 & mid.a0) | (up.a0 & dn.a0) | (mid.a0 & dn.a0);
-    const uint32_t x = up.a1 ^ mid.a1 ^ dn.a1;
-    const uint32_t y = (up.a1 & mid.a1) | (up.a1 & dn.a1) | (mid.a1 & dn.a1);
-    const uint32_t s1 = x ^ c1, z = x & c1;
-    const uint32_t s2 = y ^ z;
+    const uint32_t s0 = lop3<XOR3>(up.a0, mid.a0, dn.a0);
+    const uint32_t c1 = lop3<MAJ3>(up.a0, mid.a0, dn.a0);
+    const uint32_t x = lop3<XOR3>(up.a1, mid.a1, dn.a1);
+    const uint32_t y = lop3<MAJ3>(up.a1, mid.a1, dn.a1);
+    const uint32_t s1 = x ^ c1;
+    const uint32_t s2 = lop3<0x78>(y, x, c1);  // y ^ (x & c1)
     const uint32_t c = mid.w;
     if (RULE == APPFIS_GB_LIFE_REFERENCE) {
-        const uint32_t eq3 = ~s2 & s1 & s0;
-        const uint32_t in345 = eq3 | (s2 & ~s1);
-        return (c & in345 & o) | (~c & (eq3 | o));
+        const uint32_t in345 = lop3<0x38>(s2, s1, s0);  // S in 3..5: (~s2 & s1 & s0) | (s2 & ~s1)
+        const uint32_t d = lop3<0xD0>(in345, c, s2);    // live: S in 3..5; dead: S == 3
+        return lop3<0x8E>(c, o, d);                      // c ? o & d : o | d
     } else {
-        const uint32_t in34 = (~s2 & s1 & s0) | (s2 & ~s1 & ~s0);
-        return in34 & (c | ~s2);
+        const uint32_t in34 = lop3<0x18>(s2, s1, s0);   // S in 3..4
+        return lop3<0xD0>(in34, c, s2);                  // live: S in 3..4; dead: S == 3
     }
 }
 struct RawBits {
@@ -276,8 +287,8 @@ __device__ __forceinline__ RowBits tile_row(uint32_t w)
     const uint32_t L = __funnelshift_l(lw, w, 1), R = __funnelshift_r(w, rw, 1);
     RowBits r;
     r.w = w;
-    r.a0 = L ^ w ^ R;
-    r.a1 = (L & w) | (R & (L ^ w));
+    r.a0 = lop3<XOR3>(L, w, R);
+    r.a1 = lop3<MAJ3>(L, w, R);
     return r;
 }
 
