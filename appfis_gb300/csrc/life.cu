@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(TB_WARPS * 32) life_bits_tb(const uint32_t* __
             if (r0 < r1) {
                 RowBits up = tile_row(cur[r0 - 1][lane]);
                 RowBits mid = tile_row(cur[r0][lane]);
-#pragma unroll 4  // 4 rows per trip: the up/mid/dn rotation becomes register renaming
+#pragma unroll 8  // 8 rows per trip: the up/mid/dn rotation becomes register renaming
                 for (int r = r0; r < r1; r++) {
                     const RowBits dn = tile_row(cur[r + 1][lane]);
                     const uint32_t o = RULE == APPFIS_GB_LIFE_REFERENCE ? old[r][lane] : 0u;
