@@ -3,9 +3,9 @@
 // for the per-face / per-cell arithmetic and the reference it follows.
 //
 // One cooperative launch advances a batch of independent domains of uneven sizes to t_end.
-// Work items are strips (SCOLS interior columns x ROWS rows) of all domains; in each phase warps
-// take them one at a time from a counter (a strip's cost follows the water, so a fixed stride
-// leaves some warps with far more wet strips than others).
+// Work items are strips (SCOLS interior columns x ROWS rows) of all domains; in each phase a warp
+// takes its first strip by index and the rest one at a time from a counter (a strip's cost
+// follows the water, so a fixed stride leaves some warps with far more wet strips than others).
 // Each step is phase A (wet/dry fix of the previous step + CFL dt, min per domain) and phase B
 // (fluxes + update into the other state buffer), separated by grid barriers whose spin waits
 // are bounded (on timeout the kernel records an error and returns).  Per-domain scalars
