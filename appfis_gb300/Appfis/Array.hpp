@@ -43,6 +43,7 @@ namespace APPFIS
 		int _size = 0;
 		int _dims[3] = { 1, 1, 1 };
 		bool _owner = false;
+		bool _device = false;  // a grid's view of its device buffer (set by Grid::Upload)
 
 	public:
 		Array() {}
@@ -106,6 +107,8 @@ namespace APPFIS
 		int* GetDims() const { return const_cast<int*>(_dims); }
 		T* GetData() { return _data; }
 		bool IsOwner() const { return _owner; }
+		bool IsDeviceView() const { return _device; }
+		void MarkDeviceView() { _device = true; }
 
 		ArrayArg<T> Arg() const
 		{
@@ -140,6 +143,7 @@ namespace APPFIS
 			if (_owner && _data) delete[] _data;
 			_data = nullptr;
 			_owner = false;
+			_device = false;
 			_nDim = 0;
 			_size = 0;
 			_dims[0] = _dims[1] = _dims[2] = 1;
@@ -267,6 +271,7 @@ namespace APPFIS
 			for (int a = 0; a < 3; a++) _dims[a] = o._dims[a];
 			_data = nullptr;
 			_owner = false;
+			_device = o._device && !o._owner;
 			if (o._data != nullptr && o._owner)
 			{
 				AllocateMemory();

@@ -174,6 +174,7 @@ namespace APPFIS
 				if (!_dev[b]) CheckCuda(cudaMalloc((void**)&_dev[b], bytes > 0 ? bytes : sizeof(T)), "cudaMalloc(grid)");
 				CheckCuda(cudaMemcpyAsync(_dev[b], _host[b].GetData(), bytes, cudaMemcpyHostToDevice, st), "upload");
 				_view[b] = Array<T>(_dev[b], _nDim, _host[b].GetSize(), _host[b].GetDims());
+				_view[b].MarkDeviceView();
 			}
 			if (_type != DUAL)
 			{

@@ -55,6 +55,7 @@ namespace APPFIS
 			typedef ArrayArg<U> type;
 			static ArrayArg<U> to(Array<U>* a)
 			{
+				if (a != nullptr && a->IsDeviceView()) return a->Arg();  // a grid's device view: no driver query
 				cudaPointerAttributes attr;
 				if (a == nullptr || a->GetData() == nullptr || cudaPointerGetAttributes(&attr, a->GetData()) != cudaSuccess ||
 					attr.type != cudaMemoryTypeDevice)
@@ -94,9 +95,9 @@ namespace APPFIS
 
 		// Rows (2-D) or planes (3-D) per thread: a thread calls the functor for MARCH consecutive
 		// points along its slowest axis, so the neighbour values of one call are in L1 for the next.
-		// Every point of the box is still visited exactly once, in no particular order.  In 3-D the
-		// march pays only for functors over a few fields (measured on GB300: the radius-4 star over
-		// 2 arrays 107 -> 139 GLUP/s; Himeno over 14 arrays 68 -> 48, its loads in flight are what
+		// Every point of the box is still visited exactly once, in no particular order.  The march
+		// pays only for functors over a few fields (measured on GB300: the radius-4 star over 2
+		// arrays 107 -> 139 GLUP/s; Himeno over 14 arrays 68 -> 48, its loads in flight are what
 		// count), so functors taking more than MARCH_MAX_ARRAYS arrays keep one point per thread.
 		constexpr int MARCH = 4, MARCH_MAX_ARRAYS = 4;
 
@@ -108,13 +109,13 @@ namespace APPFIS
 			static const int value = IsArrayArg<H>::value + ArrayCount<R...>::value;
 		};
 
-		template<class... A>
+		template<int M, class... A>
 		__global__ void Functor2D(int x0, int x1, int y0, int y1, A... args)
 		{
 			const int i = x0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-			const int jb = y0 + (int)(blockIdx.y * blockDim.y + threadIdx.y) * MARCH;
+			const int jb = y0 + (int)(blockIdx.y * blockDim.y + threadIdx.y) * M;
 			if (i >= x1) return;
-			for (int j = jb; j < jb + MARCH && j < y1; j++) STENCIL(i, j, Holder<A>(args).get()...);
+			for (int j = jb; j < jb + M && j < y1; j++) STENCIL(i, j, Holder<A>(args).get()...);
 		}
 
 		template<int M, class... A>
@@ -203,8 +204,10 @@ namespace APPFIS
 		const int x0 = config.GetStartX(), x1 = config.GetEndX(), y0 = config.GetStartY(), y1 = config.GetEndY();
 		if (x1 > x0 && y1 > y0)
 		{
-			dim3 blk(32, 8), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 8 * detail::MARCH));
-			detail::Functor2D<typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
+			constexpr int M =
+				detail::ArrayCount<typename detail::KArg<TArgs>::type...>::value <= detail::MARCH_MAX_ARRAYS ? detail::MARCH : 1;
+			dim3 blk(32, 8), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 8 * M));
+			detail::Functor2D<M, typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
 				x0, x1, y0, y1, detail::KArg<TArgs>::to(args)...);
 		}
 		detail::AfterSweep(config);

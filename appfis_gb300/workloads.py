@@ -178,3 +178,34 @@ def triton_domain(ny, nx, seed, beta=-2.5, relief=50.0, h0=1.0, area=0.05):
 def triton_batch(n=32, lo=512, hi=3072, seed=42, **kw):
     """List of (dem, h) FP64 interiors for the batched workload."""
     return [triton_domain(ny, nx, seed + 1000 * (d + 1), **kw) for d, (ny, nx) in enumerate(triton_sizes(n, lo, hi, seed))]
+
+
+def write_triton_case(d, nx, ny, seed, duration):
+    """The Triton application's input files for one synthetic domain, in directory d: case.cfg
+    (key=value), dem.asc (ASCII grid with its 6-line header, dx = 10 m), h.asc (initial depth),
+    hydro.txt (a point-source hydrograph) and src.txt (the source at the domain centre), the
+    formats the application's readers take (Triton/src/config_utils.hpp, triton_appfis.hpp,
+    inflow.hpp).  Values are printed with 6 decimals."""
+    import os
+
+    dem, h = triton_domain(ny, nx, seed)
+
+    def grid(path, a, header=""):
+        with open(path, "w") as f:
+            f.write(header)
+            np.savetxt(f, a, fmt="%.6f", delimiter=" ")
+
+    grid(os.path.join(d, "dem.asc"), dem,
+         "ncols %d\nnrows %d\nxllcorner 0.0\nyllcorner 0.0\ncellsize 10.0\nNODATA_value -9999\n" % (nx, ny))
+    grid(os.path.join(d, "h.asc"), h)
+    with open(os.path.join(d, "hydro.txt"), "w") as f:
+        f.write("% time (hr), flow (m3/s)\n0, 0\n0.01, 8.0\n0.03, 3.0\n1.0, 0.0\n")
+    with open(os.path.join(d, "src.txt"), "w") as f:
+        f.write("%% x, y\n%.1f, %.1f\n" % (10.0 * (nx // 2) - 5.0, 10.0 * (ny // 2) - 5.0))
+    cfg = dict(dem_filename="dem.asc", h_infile="h.asc", hydrograph_filename="hydro.txt", src_loc_file="src.txt",
+               num_sources=1, const_mann=0.035, time_step=1.0, time_increment_fixed=0, time_series_flag=0, courant=0.5,
+               hextra=0.001, gpu_direct_flag=0, num_runoffs=0, num_extbc=0, print_option="h", input_format="ASC",
+               output_format="ASC", output_option="SEQ", sim_start_time=0, sim_duration=duration, print_interval=60)
+    with open(os.path.join(d, "case.cfg"), "w") as f:
+        f.write("".join("%s=%s\n" % kv for kv in cfg.items()))
+

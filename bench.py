@@ -240,7 +240,8 @@ def apps_unchanged():
     reference's CPU path (OpenMP, every core), the reference's own GPU path (APPFIS_CUDA for
     sm_103a) and the drop-in headers (generic functor kernels of this engine; both GPU builds
     with nvcc's default FMA contraction).  GLUP/s from each
-    application's own COMPUTE timer (its printed `Compute:` seconds)."""
+    application's own COMPUTE timer (its printed `Compute:` seconds; the flood application: its `BLUPS:`
+    line, since its step count follows the time step)."""
     import re
     from concurrent.futures import ThreadPoolExecutor
 
@@ -250,7 +251,10 @@ def apps_unchanged():
     cases = [("HeatDiffusion", ["-dimx=256", "-dimy=256", "-dimz=256", "-iteration=100"], 256 ** 3 * 100),
              ("GameOfLife", ["-dimx=4096", "-dimy=4096", "-iteration=200"], 4096 ** 2 * 200),
              ("Himeno", ["-dimx=129", "-dimy=129", "-dimz=257", "-iteration=100"], 129 * 129 * 257 * 100),
-             ("FDTD3d", ["-dimx=256", "-dimy=256", "-dimz=256", "-iteration=50"], 256 ** 3 * 50)]
+             ("FDTD3d", ["-dimx=256", "-dimy=256", "-dimz=256", "-iteration=50"], 256 ** 3 * 50),
+             # the flood application on a 1024^2 synthetic case to 600 s (FP64; its step count follows
+             # the CFL time step, so GLUP/s is the application's own BLUPS line)
+             ("Triton", ["case.cfg"], None)]
     apps = [c[0] for c in cases]
     with ThreadPoolExecutor(max_workers=8) as ex:
         ref = dict(zip(apps, ex.map(build_ref.app_ref_exe, apps)))
@@ -258,18 +262,21 @@ def apps_unchanged():
     gbx = build_apps.build(apps, exact=False)  # nvcc's default contraction, like the reference's GPU build
     cores = os.cpu_count() or 1
     out = {}
+    from appfis_gb300 import workloads as W
     with tempfile.TemporaryDirectory() as td:
+        W.write_triton_case(td, 1024, 1024, 11, 600)
         for app, args, lups in cases:
-            row = {"args": " ".join(args)}
+            row = {"args": " ".join(args) if lups else "1024x1024 synthetic case (fractal DEM, point source), 600 s"}
             for name, exe, extra in (("reference_cpu", ref[app], ["-thread=%d" % cores]), ("reference_gpu", refgpu[app], []),
                                      ("dropin_gpu", gbx[app], [])):
                 r = subprocess.run([exe] + args + extra, capture_output=True, text=True, timeout=900, cwd=td)
                 m = re.search(r"^Compute:\s*(\S+)", r.stdout, re.M)
-                if r.returncode != 0 or not m:
+                b = re.search(r"^BLUPS:\s*(\S+)", r.stdout, re.M)
+                if r.returncode != 0 or not m or (lups is None and not b):
                     row[name] = {"error": (r.stderr or r.stdout)[-300:]}
                     continue
                 secs = float(m.group(1))
-                row[name] = {"compute_s": secs, "glups": lups / secs / 1e9}
+                row[name] = {"compute_s": secs, "glups": lups / secs / 1e9 if lups else float(b.group(1))}
             out[app] = row
     return {"apps_unchanged": out, "cores": cores}
 

@@ -74,30 +74,6 @@ def test_fdtd_application_runs(exes, tmp_path):
     assert re.search(r"^GFLOPS:\s*\S+", out, re.M)
 
 
-def _write_grid(path, a, header=""):
-    with open(path, "w") as f:
-        f.write(header)
-        for row in a:
-            f.write(" ".join("%.6f" % v for v in row) + "\n")
-
-
-def _triton_case(d, nx, ny, seed, duration):
-    dem, h = W.triton_domain(ny, nx, seed)
-    _write_grid(os.path.join(d, "dem.asc"), dem,
-                "ncols %d\nnrows %d\nxllcorner 0.0\nyllcorner 0.0\ncellsize 10.0\nNODATA_value -9999\n" % (nx, ny))
-    _write_grid(os.path.join(d, "h.asc"), h)
-    with open(os.path.join(d, "hydro.txt"), "w") as f:
-        f.write("% time (hr), flow (m3/s)\n0, 0\n0.01, 8.0\n0.03, 3.0\n1.0, 0.0\n")
-    with open(os.path.join(d, "src.txt"), "w") as f:
-        f.write("%% x, y\n%.1f, %.1f\n" % (10.0 * (nx // 2) - 5.0, 10.0 * (ny // 2) - 5.0))
-    cfg = dict(dem_filename="dem.asc", h_infile="h.asc", hydrograph_filename="hydro.txt", src_loc_file="src.txt",
-               num_sources=1, const_mann=0.035, time_step=1.0, time_increment_fixed=0, time_series_flag=0, courant=0.5,
-               hextra=0.001, gpu_direct_flag=0, num_runoffs=0, num_extbc=0, print_option="h", input_format="ASC",
-               output_format="ASC", output_option="SEQ", sim_start_time=0, sim_duration=duration, print_interval=60)
-    with open(os.path.join(d, "case.cfg"), "w") as f:
-        f.write("".join("%s=%s\n" % kv for kv in cfg.items()))
-
-
 @pytest.mark.parametrize("nx,ny,seed,duration", [(48, 40, 77, 120), (97, 61, 5, 90)])
 def test_triton_application_case_files(exes, tmp_path, nx, ny, seed, duration):
     gbx, ref = exes
@@ -105,7 +81,7 @@ def test_triton_application_case_files(exes, tmp_path, nx, ny, seed, duration):
     for name, exe, extra in (("gb", gbx["Triton"], []), ("ref", ref["Triton"], ["-thread=4"])):
         d = tmp_path / name
         d.mkdir()
-        _triton_case(str(d), nx, ny, seed, duration)
+        W.write_triton_case(str(d), nx, ny, seed, duration)
         text = run(exe, ["case.cfg", "-output"] + extra, str(d))
         steps = int(re.search(r"^Number of iteration:\s*(\d+)", text, re.M).group(1))
         fields = [np.loadtxt(str(d / "output" / f)) for f in ("h.txt", "u.txt", "v.txt")]
