@@ -21,7 +21,8 @@ namespace {
 
 constexpr uint32_t FULL = 0xffffffffu;
 constexpr uint32_t LSB = 0x01010101u;  // bit 0 of each byte
-constexpr int LIFE_ROWS = 32;           // rows per warp task
+constexpr int LIFE_ROWS = 32;           // rows per warp task (bit-packed sweep)
+constexpr int U8_ROWS = 16;             // rows per warp task (u8 sweep: 4, 8, 32, 128 measured slower on 16384^2)
 
 // ------------------------------------------------------------------------------ rule logic
 // Per byte lane (u8 form): cnt in 0..8 in each byte, c/o in {0,1} per byte.
@@ -99,7 +100,7 @@ __device__ __forceinline__ RowU8 finish_row_u8(const RawU8& raw, int x0, int nx,
     return r;
 }
 
-// Warp tasks: a 512-byte strip (32 lanes x 16 cells) over LIFE_ROWS rows, visited grid-stride by
+// Warp tasks: a 512-byte strip (32 lanes x 16 cells) over U8_ROWS rows, visited grid-stride by
 // a grid sized to the resident capacity.  The loads of rows j+3 (cur) and j+2 (old) are issued
 // before row j is computed, so three rows of loads are in flight per lane.
 template <int RULE>
@@ -112,7 +113,7 @@ __global__ void __launch_bounds__(256) life_u8_swar(const uint8_t* __restrict__ 
         const int strip = task % strips, seg = task / strips;
         const int x0 = strip * 512 + lane * 16;
         const bool active = x0 < nx;
-        const int j0 = seg * LIFE_ROWS, j1 = min(j0 + LIFE_ROWS, ny);
+        const int j0 = seg * U8_ROWS, j1 = min(j0 + U8_ROWS, ny);
         RowU8 up = finish_row_u8(load_raw_u8(cur, nx, j0 == 0 ? ny - 1 : j0 - 1, x0, active, lane), x0, nx, lane);
         RowU8 mid = finish_row_u8(load_raw_u8(cur, nx, j0, x0, active, lane), x0, nx, lane);
         // two rows of loads in flight: cur rows j+1, j+2 and old rows j, j+1
@@ -430,7 +431,7 @@ int run_u8(uint8_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStream
     int ci = 0;
     if (nx % 16 == 0) {
         const int strips = (nx + 511) / 512;
-        const int tasks = strips * ((ny + LIFE_ROWS - 1) / LIFE_ROWS);
+        const int tasks = strips * ((ny + U8_ROWS - 1) / U8_ROWS);
         const unsigned grid = resident_grid(life_u8_swar<RULE>, tasks);
         for (int g = 0; g < gens; g++) {
             life_u8_swar<RULE><<<grid, 256, 0, st>>>(buf[ci], buf[1 - ci], nx, ny, strips, tasks);
