@@ -10,19 +10,19 @@
 // generation, Appfis/Communication.hpp:612-678) becomes index wrap-around inside the sweep.
 //
 // Layout: interior cells only, x fastest, row pitch nx bytes (u8) or nx/32 words (bits).
-// The one-generation sweeps (life_u8_swar, life_bits_sweep) march down a strip of rows per warp,
-// keeping the row above / at / below in registers (each row is loaded once per warp task) and
-// exchanging the words at lane boundaries with warp shuffles; only the two end lanes load one
-// extra word per row.  Runs of 16 or more bit-packed generations use life_bits_tb, which
+// The byte-per-cell sweep (life_u8_bulk) stages its rows in shared memory with bulk copies; the
+// one-generation bit-packed sweep (life_bits_sweep) marches down a strip of rows per warp,
+// keeping the row above / at / below in registers and exchanging the words at lane boundaries
+// with warp shuffles.  Runs of 16 or more bit-packed generations use life_bits_tb, which
 // advances a tile held in shared memory by 16 generations per launch.
 #include "gb_common.cuh"
+#include "tma.cuh"
 
 namespace {
 
 constexpr uint32_t FULL = 0xffffffffu;
 constexpr uint32_t LSB = 0x01010101u;  // bit 0 of each byte
 constexpr int LIFE_ROWS = 32;           // rows per warp task (bit-packed sweep)
-constexpr int U8_ROWS = 16;             // rows per warp task (u8 sweep: 4, 8, 32, 128 measured slower on 16384^2)
 
 // ------------------------------------------------------------------------------ rule logic
 // Per byte lane (u8 form): cnt in 0..8 in each byte, c/o in {0,1} per byte.
@@ -58,97 +58,117 @@ __global__ void life_u8_generic(const uint8_t* __restrict__ cur, uint8_t* __rest
 }
 
 // ------------------------------------------------------------------------------ u8 SWAR form
-struct RawU8 {    // one row's loads for this lane, before the lane-boundary exchange
-    uint4 v;      // the 16 cells of this lane
-    uint32_t lw;  // lane 0: cell x0-1 in the top byte
-    uint32_t rw;  // last active lane: cell x0+16 in the low byte
-};
 struct RowU8 {
     uint32_t w[4];   // the 16 cells of this lane
     uint32_t s3[4];  // per byte: left + self + right
 };
 
-__device__ __forceinline__ RawU8 load_raw_u8(const uint8_t* __restrict__ cur, int nx, int row, int x0, bool active, int lane)
-{
-    const uint8_t* p = cur + (size_t)row * nx;
-    RawU8 r;
-    r.v = active ? __ldg(reinterpret_cast<const uint4*>(p + x0)) : make_uint4(0, 0, 0, 0);
-    r.lw = lane == 0 ? (uint32_t)__ldg(p + (x0 == 0 ? nx - 1 : x0 - 1)) << 24 : 0u;
-    r.rw = (active && (lane == 31 || x0 + 16 >= nx)) ? (uint32_t)__ldg(p + (x0 + 16 >= nx ? 0 : x0 + 16)) : 0u;
-    return r;
-}
+// ------------------------------------------------------------------------------ u8 form, bulk-staged
+// A CTA owns a strip of UB_W cells (256 threads x 16) of UB_ROWS consecutive rows.  Each row it
+// needs arrives in a shared-memory slot by bulk copies (the cur row with a 16-byte periodic halo
+// on each side, and for output rows the t-1 row), UB_RING - 1 rows ahead of the row it computes,
+// signalled on the slot's mbarrier: every copy is a contiguous run of up to 4 KB, and the rows in
+// flight need no registers.  Each thread carries the row summaries of the rows above and at its
+// output row and reads the row below from the slot (one 16-byte vector and the two neighbour
+// words), so every row is summarised once.  Waits are bounded; a wait that gives up sets the
+// device status word.
+constexpr int UB_W = 4096;      // strip width in cells (bytes)
+constexpr int UB_ROWS = 32;     // output rows per CTA
+constexpr int UB_RING = 6;      // row slots
+constexpr int UB_OLD = 16 + UB_W + 16;      // offset of the t-1 row in a slot
+constexpr int UB_SLOT = UB_OLD + UB_W;      // 8224 bytes
+constexpr int UB_SMEM = UB_RING * UB_SLOT + UB_RING * 8;
 
-__device__ __forceinline__ RowU8 finish_row_u8(const RawU8& raw, int x0, int nx, int lane)
+__device__ __forceinline__ RowU8 slot_row_u8(const unsigned char* s, int t)
 {
-    uint32_t lw = __shfl_up_sync(FULL, raw.v.w, 1);
-    uint32_t rw = __shfl_down_sync(FULL, raw.v.x, 1);
-    if (lane == 0) lw = raw.lw;
-    if (lane == 31 || x0 + 16 >= nx) rw = raw.rw;
+    const unsigned char* p = s + 16 + 16 * t;
+    const uint4 v = *reinterpret_cast<const uint4*>(p);
+    const uint32_t lw = *reinterpret_cast<const uint32_t*>(p - 4);   // cell x-1 in the top byte
+    const uint32_t rw = *reinterpret_cast<const uint32_t*>(p + 16);  // cell x+16 in the low byte
     RowU8 r;
-    r.w[0] = raw.v.x;
-    r.w[1] = raw.v.y;
-    r.w[2] = raw.v.z;
-    r.w[3] = raw.v.w;
+    r.w[0] = v.x;
+    r.w[1] = v.y;
+    r.w[2] = v.z;
+    r.w[3] = v.w;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        uint32_t prev = k == 0 ? lw : r.w[k - 1];
-        uint32_t next = k == 3 ? rw : r.w[k + 1];
-        uint32_t L = __funnelshift_l(prev, r.w[k], 8);  // (w << 8) | (prev >> 24)
-        uint32_t R = __funnelshift_r(r.w[k], next, 8);  // (w >> 8) | (next << 24)
-        r.s3[k] = L + r.w[k] + R;
+        const uint32_t prev = k == 0 ? lw : r.w[k - 1];
+        const uint32_t next = k == 3 ? rw : r.w[k + 1];
+        r.s3[k] = __funnelshift_l(prev, r.w[k], 8) + r.w[k] + __funnelshift_r(r.w[k], next, 8);
     }
     return r;
 }
 
-// Warp tasks: a 512-byte strip (32 lanes x 16 cells) over U8_ROWS rows, visited grid-stride by
-// a grid sized to the resident capacity.  The loads of rows j+3 (cur) and j+2 (old) are issued
-// before row j is computed, so three rows of loads are in flight per lane.
 template <int RULE>
-__global__ void __launch_bounds__(256) life_u8_swar(const uint8_t* __restrict__ cur, uint8_t* __restrict__ out,
-                                                     int nx, int ny, int strips, int tasks)
+__global__ void __launch_bounds__(256) life_u8_bulk(const uint8_t* __restrict__ cur, uint8_t* __restrict__ out, int nx, int ny,
+                                                     int strips, unsigned* __restrict__ status)
 {
-    const int lane = threadIdx.x & 31;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < tasks; task += nwarps) {
-        const int strip = task % strips, seg = task / strips;
-        const int x0 = strip * 512 + lane * 16;
-        const bool active = x0 < nx;
-        const int j0 = seg * U8_ROWS, j1 = min(j0 + U8_ROWS, ny);
-        RowU8 up = finish_row_u8(load_raw_u8(cur, nx, j0 == 0 ? ny - 1 : j0 - 1, x0, active, lane), x0, nx, lane);
-        RowU8 mid = finish_row_u8(load_raw_u8(cur, nx, j0, x0, active, lane), x0, nx, lane);
-        // two rows of loads in flight: cur rows j+1, j+2 and old rows j, j+1
-        const RawU8 zero = {make_uint4(0, 0, 0, 0), 0u, 0u};
-        RawU8 r1 = load_raw_u8(cur, nx, j0 + 1 >= ny ? j0 + 1 - ny : j0 + 1, x0, active, lane);
-        RawU8 r2 = j0 + 1 < j1 ? load_raw_u8(cur, nx, j0 + 2 >= ny ? j0 + 2 - ny : j0 + 2, x0, active, lane) : zero;
-        const bool ref = RULE == APPFIS_GB_LIFE_REFERENCE && active;
-        uint4 o0 = ref ? *reinterpret_cast<const uint4*>(out + (size_t)j0 * nx + x0) : make_uint4(0, 0, 0, 0);
-        uint4 o1 = (ref && j0 + 1 < j1) ? *reinterpret_cast<const uint4*>(out + (size_t)(j0 + 1) * nx + x0) : make_uint4(0, 0, 0, 0);
-        for (int j = j0; j < j1; j++) {
-            RawU8 r3 = zero;
-            uint4 o2 = make_uint4(0, 0, 0, 0);
-            if (j + 2 < j1) {  // prefetch (warp-uniform)
-                const int rr = j + 3 >= ny ? j + 3 - ny : j + 3;
-                r3 = load_raw_u8(cur, nx, rr, x0, active, lane);
-                if (ref) o2 = *reinterpret_cast<const uint4*>(out + (size_t)(j + 2) * nx + x0);
-            }
-            const RowU8 dn = finish_row_u8(r1, x0, nx, lane);
-            if (active) {
-                const uint32_t ow[4] = {o0.x, o0.y, o0.z, o0.w};
-                uint32_t nw[4];
+    extern __shared__ __align__(128) unsigned char ub[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(ub + UB_RING * UB_SLOT);
+    const int t = threadIdx.x;
+    const int strip = blockIdx.x % strips, band = blockIdx.x / strips;
+    const int x0 = strip * UB_W, w = min(UB_W, nx - x0);
+    const int j0 = band * UB_ROWS, j1 = min(j0 + UB_ROWS, ny);
+    const int rbase = j0 - 1;  // row of slot 0, first use
+    const bool active = 16 * t < w;
+    if (gb::tma::smem_u32(ub) & 15u) {
+        if (t == 0) atomicOr(status, (unsigned)gb::ST_SMEM_ALIGN);
+        return;
+    }
+    if (t == 0) {
+        for (int n = 0; n < UB_RING; n++) gb::tma::bar_init(&bar[n], 1);
+        gb::tma::fence_init();
+    }
+    __syncthreads();
+    int last_issued = rbase - 1;  // thread 0 only
+    auto issue = [&](int r) {     // cur row r (periodic) with its halos; the t-1 row if r is an output row
+        last_issued = r;
+        const int n = (r - rbase) % UB_RING;
+        unsigned char* d = ub + n * UB_SLOT;
+        const int rr = r < 0 ? r + ny : (r >= ny ? r - ny : r);
+        const uint8_t* row = cur + (size_t)rr * nx;
+        const bool oldrow = RULE == APPFIS_GB_LIFE_REFERENCE && r >= j0 && r < j1;
+        gb::tma::arrive_expect(&bar[n], 32 + w + (oldrow ? w : 0));
+        gb::tma::load_1d(d, row + (x0 == 0 ? nx - 16 : x0 - 16), 16, &bar[n]);
+        gb::tma::load_1d(d + 16, row + x0, w, &bar[n]);
+        gb::tma::load_1d(d + 16 + w, row + (x0 + w == nx ? 0 : x0 + w), 16, &bar[n]);
+        if (oldrow) gb::tma::load_1d(d + UB_OLD, out + (size_t)r * nx + x0, w, &bar[n]);
+    };
+    auto ready = [&](int r, uint64_t limit = 1000000000ull) {
+        return gb::tma::wait(&bar[(r - rbase) % UB_RING], (unsigned)((r - rbase) / UB_RING) & 1u, limit);
+    };
+    auto slot = [&](int r) { return ub + ((r - rbase) % UB_RING) * UB_SLOT; };
+    if (t == 0)
+        for (int r = rbase; r < rbase + UB_RING && r <= j1; r++) issue(r);
+    bool bad = !ready(rbase) || !ready(j0);
+    RowU8 up = slot_row_u8(slot(rbase), t);
+    RowU8 mid = slot_row_u8(slot(j0), t);
+    bad = __syncthreads_or(bad);  // row j0-1 is read: its slot takes row j0-1+UB_RING
+    if (t == 0 && !bad && rbase + UB_RING <= j1) issue(rbase + UB_RING);
+    for (int j = j0; j < j1 && !bad; j++) {
+        if (!ready(j + 1)) bad = true;
+        const RowU8 dn = slot_row_u8(slot(j + 1), t);
+        const uint4 o = RULE == APPFIS_GB_LIFE_REFERENCE ? *reinterpret_cast<const uint4*>(slot(j) + UB_OLD + 16 * t)
+                                                         : make_uint4(0, 0, 0, 0);
+        if (active && !bad) {
+            const uint32_t ow[4] = {o.x, o.y, o.z, o.w};
+            uint32_t nw[4];
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    const uint32_t cnt = up.s3[k] + (mid.s3[k] - mid.w[k]) + dn.s3[k];
-                    nw[k] = rule_bytes<RULE>(cnt, mid.w[k], ow[k]);
-                }
-                *reinterpret_cast<uint4*>(out + (size_t)j * nx + x0) = make_uint4(nw[0], nw[1], nw[2], nw[3]);
+            for (int k = 0; k < 4; k++) {
+                const uint32_t cnt = up.s3[k] + (mid.s3[k] - mid.w[k]) + dn.s3[k];
+                nw[k] = rule_bytes<RULE>(cnt, mid.w[k], ow[k]);
             }
-            up = mid;
-            mid = dn;
-            r1 = r2;
-            r2 = r3;
-            o0 = o1;
-            o1 = o2;
+            *reinterpret_cast<uint4*>(out + (size_t)j * nx + x0 + 16 * t) = make_uint4(nw[0], nw[1], nw[2], nw[3]);
         }
+        up = mid;
+        mid = dn;
+        // row j's slot (cur read at step j-1, t-1 read now) takes row j + UB_RING
+        bad = __syncthreads_or(bad);
+        if (t == 0 && !bad && j + UB_RING <= j1) issue(j + UB_RING);
+    }
+    if (bad && t == 0) {  // a wait gave up: report and let the copies still in flight land
+        atomicOr(status, (unsigned)gb::ST_TMA_TIMEOUT);
+        for (int r = max(rbase, last_issued - UB_RING + 1); r <= last_issued; r++) ready(r, gb::tma::DRAIN_NS);
     }
 }
 
@@ -430,11 +450,13 @@ int run_u8(uint8_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStream
 {
     int ci = 0;
     if (nx % 16 == 0) {
-        const int strips = (nx + 511) / 512;
-        const int tasks = strips * ((ny + U8_ROWS - 1) / U8_ROWS);
-        const unsigned grid = resident_grid(life_u8_swar<RULE>, tasks);
+        unsigned* status;
+        GB_TRY(gb::status_word(&status));
+        GB_CUDA(cudaFuncSetAttribute(life_u8_bulk<RULE>, cudaFuncAttributeMaxDynamicSharedMemorySize, UB_SMEM));
+        const int strips = (nx + UB_W - 1) / UB_W;
+        const unsigned grid = (unsigned)strips * gb::ceil_div(ny, UB_ROWS);
         for (int g = 0; g < gens; g++) {
-            life_u8_swar<RULE><<<grid, 256, 0, st>>>(buf[ci], buf[1 - ci], nx, ny, strips, tasks);
+            life_u8_bulk<RULE><<<grid, 256, UB_SMEM, st>>>(buf[ci], buf[1 - ci], nx, ny, strips, status);
             ci = 1 - ci;
         }
     } else {

@@ -66,6 +66,15 @@ __device__ __forceinline__ void load_3d(void* dst, const CUtensorMap* map, int x
         : "memory");
 }
 
+// Copies `bytes` (a multiple of 16) from global src to shared dst, both 16-byte aligned, as one
+// bulk copy; completion is signalled on `bar` as transaction bytes.
+__device__ __forceinline__ void load_1d(void* dst, const void* src, unsigned bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+                 "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
 __device__ __forceinline__ void prefetch_map(const CUtensorMap* map)
 {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");

@@ -770,7 +770,7 @@ def profile_small(name, torch, gb, W, dev, sp):
 def profile_case(name, local):
     """Short fixed launch sequences for ncu captures.
     life:   16384^2 GameOfLife, 20 bit-packed generations (one life_bits_tb launch of 16 + 4
-            life_bits_sweep) then 20 u8 sweeps (life_u8_swar)
+            life_bits_sweep) then 20 u8 sweeps (life_u8_bulk)
     himeno: 257x257x513 (rows padded to 264), 5 plain sweeps (himeno_tma<0>), 5 mixed sweeps
             (himeno_tma<1>, himeno_correct)
     fdtd:   512^3, 5 FP32 steps then 5 FP16 steps (star_r4_tma)

@@ -14,7 +14,7 @@ sys.path.insert(0, ROOT)
 import bench  # noqa: E402
 
 
-@pytest.mark.parametrize("kernel", ["life_bits_tb", "life_u8_swar", "heat2d_regs", "himeno_tma<plain>", "himeno_mixed2",
+@pytest.mark.parametrize("kernel", ["life_bits_tb", "life_u8_bulk", "heat2d_regs", "himeno_tma<plain>", "himeno_mixed2",
                                     "star_r4_tma<float>", "star_r4_tma<half>"])
 def test_profiled_traffic_present(kernel):
     t = bench.profiled_traffic(kernel)
