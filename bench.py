@@ -453,7 +453,8 @@ def run_ours(args, rank, world, local):
         "forms": {
             "bits": {"glups": value, "ms_per_step": ms_bits, "kernel_ms": bits_ms, "achieved_gbs": bits_achieved},
             "u8": {"glups": N * gens / (ms_u8 * 1e-3) / 1e9 * world, "ms_per_step": ms_u8, "kernel_ms": u8_ms,
-                   "achieved_gbs": u8_achieved, "frac": u8_achieved / hbm_peak, "bytes_per_lup": 3},
+                   "kernel": "life_u8_bulk", "achieved_gbs": u8_achieved, "frac": u8_achieved / hbm_peak,
+                   "bytes_per_lup": 3, "traffic": profiled_traffic("life_u8_bulk")},
         },
         "clocks": clocks,
     }
