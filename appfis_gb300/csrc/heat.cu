@@ -34,7 +34,8 @@ __global__ void __launch_bounds__(256) heat2d_sweep_k(const float* __restrict__ 
                         cx, cy);
 }
 
-// Overlapped tiling: output tile TX x TY, halo S (runtime, <= SMAX), S sweeps per launch.  The
+// Overlapped tiling: output tile TX x TY, halo S <= SMAX, S sweeps per launch (S is a template
+// argument: launch_heat_regs instantiates 1..SMAX and picks the launch's).  The
 // (TX + 2 SMAX) x (TY + 2 SMAX) region is cut into 4 x 4 blocks, one per thread, held in
 // registers for all S sweeps.  A sweep publishes each block's four edges (top and bottom rows,
 // left and right columns, one 16-byte vector each) into shared memory, synchronises once, reads

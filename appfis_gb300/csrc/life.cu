@@ -57,13 +57,12 @@ __global__ void life_u8_generic(const uint8_t* __restrict__ cur, uint8_t* __rest
     out[r0 + i] = (uint8_t)rule_bytes<RULE>(cnt, c, RULE == APPFIS_GB_LIFE_REFERENCE ? o : 0u);
 }
 
-// ------------------------------------------------------------------------------ u8 SWAR form
-struct RowU8 {
-    uint32_t w[4];   // the 16 cells of this lane
-    uint32_t s3[4];  // per byte: left + self + right
+// ------------------------------------------------------------------------------ u8 form, bulk-staged
+struct RowU8 {         // 16 cells of one row, one per byte (SWAR)
+    uint32_t w[4];     // the cells
+    uint32_t s3[4];    // per byte: left + self + right
 };
 
-// ------------------------------------------------------------------------------ u8 form, bulk-staged
 // A CTA owns a strip of UB_W cells (256 threads x 16) of UB_ROWS consecutive rows.  Each row it
 // needs arrives in a shared-memory slot by bulk copies (the cur row with a 16-byte periodic halo
 // on each side, and for output rows the t-1 row), UB_RING - 1 rows ahead of the row it computes,
