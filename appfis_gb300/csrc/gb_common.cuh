@@ -40,6 +40,25 @@ inline int balanced_chunk(int n, int target)
     return (n + chunks - 1) / chunks;
 }
 
+// Chunk size for a grid with `per_chunk` CTAs per chunk of planes: among the balanced chunks of
+// about lo..hi planes (steps of 8), the one whose grid fills `slots` resident CTAs best over its
+// waves, counting the `halo` planes each chunk reads beyond its own as waste.
+inline int wave_chunk(int n, int lo, int hi, long long per_chunk, long long slots, int halo)
+{
+    int best = balanced_chunk(n, lo);
+    double score = -1.0;
+    for (int t = lo; t <= hi; t += 8) {
+        const int kz = balanced_chunk(n, t), chunks = (n + kz - 1) / kz;
+        const long long ctas = per_chunk * chunks, waves = (ctas + slots - 1) / slots;
+        const double sc = (double)ctas / (double)(waves * slots) * kz / (kz + halo);
+        if (sc > score + 1e-9) {
+            score = sc;
+            best = kz;
+        }
+    }
+    return best;
+}
+
 // Number of SMs of the current device (cached).
 int sm_count();
 

@@ -815,11 +815,19 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     // TMA-staged inner sweeps (two points per thread) when the FP16 rows are 16-byte aligned
     // (pitch a multiple of 8)
     const bool use_tma = pitch % 8 == 0 && gb::aligned16(hw) && gb::aligned16(coef[3]);
-    const int tkz = gb::balanced_chunk(nz, HKZ);
+    constexpr int tsmem = mixed2_smem(MIX_S);
+    int tkz = gb::balanced_chunk(nz, HKZ);
+    if (use_tma) {  // z chunks that fill the resident CTAs in whole waves (only e re-reads a halo)
+        GB_CUDA(cudaFuncSetAttribute(himeno_mixed2<MIX_S>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem));
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, himeno_mixed2<MIX_S>, MX / 2 * MY, tsmem) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        tkz = gb::wave_chunk(nz, 32, 64, (long long)(nx / MX + 1) * gb::ceil_div(ny, MY), (long long)per_sm * gb::sm_count(), 0);
+    }
     dim3 tblk(MX / 2, MY), tgrd(nx / MX + 1, gb::ceil_div(ny, MY), gb::ceil_div(nz, tkz));
     TileMaps tmaps[2];
     unsigned* status = nullptr;
-    constexpr int tsmem = mixed2_smem(MIX_S);
     if (use_tma) {
         const int py = ny + 2;
         for (int n = 0; n < 10; n++)
@@ -831,7 +839,6 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
             GB_TRY(gb::tensor_map_3d(&tmaps[b].m[12], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, E[b], nx + 2, py, nz + 2, pitch, py, MW,
                                      MY + 2));
         GB_TRY(gb::status_word(&status));
-        GB_CUDA(cudaFuncSetAttribute(himeno_mixed2<MIX_S>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem));
     }
     double* rpartials = nullptr;
     unsigned* rticket = nullptr;

@@ -558,9 +558,17 @@ int run_star_tma(T** buf, int nx, int ny, int nz, int pitch, int iters, int mode
     constexpr int smem = Lay::smem();
     auto kern = mode == 0 ? star_r4_tma<T, 0, VXT> : star_r4_tma<T, 1, VXT>;
     GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    // default z chunk: ~48 FP32 / ~32 FP16 planes per CTA (512^3: 2816 / 4096 CTAs, several waves
-    // of 4 CTAs per SM; longer chunks re-read less halo but leave a ragged last wave)
-    const int tkz = kz > 0 ? kz : gb::balanced_chunk(nz, sizeof(T) == 4 ? 48 : 32);
+    // default z chunk: 32-64 planes per CTA, the length whose grid fills the resident CTAs in the
+    // most nearly whole waves, counting the 8 halo planes each chunk re-reads (512^3: 47 planes,
+    // 2816 CTAs in 4.6 waves of 608)
+    int tkz = kz;
+    if (tkz <= 0) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 16 * (TTY / TRY), smem) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        tkz = gb::wave_chunk(nz, 32, 64, (long long)gb::ceil_div(nx, Lay::TX) * gb::ceil_div(ny, TTY),
+                             (long long)per_sm * gb::sm_count(), 2 * R);
+    }
     dim3 blk(16, TTY / TRY), grd(gb::ceil_div(nx, Lay::TX), gb::ceil_div(ny, TTY), gb::ceil_div(nz, tkz));
     int ci = 0;
     for (int it = 0; it < iters; it++) {
@@ -626,7 +634,7 @@ int appfis_gb_star_r4(void* a, void* b, int dtype, int nx, int ny, int nz, int p
     if (tile != APPFIS_GB_STAR_AUTO && tile != APPFIS_GB_STAR_SCALAR2 && tile != APPFIS_GB_STAR_SCALAR4 &&
         tile != APPFIS_GB_STAR_TMA_X4 && tile != APPFIS_GB_STAR_TMA_X2 && tile != APPFIS_GB_STAR_VEC)
         return gb::fail(APPFIS_GB_EINVAL, "star_r4: unknown tile %d", tile);
-    const int kz = zchunk <= 0 ? 0 : zchunk;  // 0: the tile's default (TMA-staged: ~48 FP32 / ~32 FP16 planes; 32 otherwise)
+    const int kz = zchunk <= 0 ? 0 : zchunk;  // 0: the tile's default (TMA-staged: 32-64 planes chosen for whole waves; 32 otherwise)
     cudaStream_t st = gb::as_stream(stream);
     if (dtype == APPFIS_GB_F32)
         return run_star<float>((float*)a, (float*)b, nx, ny, nz, pitch, iters, mode, coeff, weights, tile, kz, cur_index, st);

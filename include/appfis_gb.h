@@ -192,7 +192,8 @@ APPFIS_GB_API int appfis_gb_himeno_job(const float* coef_host, float* p_host, in
  * dtype: APPFIS_GB_F32 or APPFIS_GB_F16 (storage).  tile selects the kernel (APPFIS_GB_STAR_*;
  * AUTO: the TMA-staged tile when rows and fields are 16-byte aligned, else the vector tile when
  * 4-element vectors are aligned, else the scalar tile; all give the same results).  zchunk: z
- * planes per CTA (0 = the tile's default: TMA-staged ~48 FP32 / ~32 FP16, balanced over nz; 32 otherwise). */
+ * planes per CTA (0 = the tile's default: TMA-staged 32-64 planes balanced over nz, the length that fills the
+ * resident CTAs in the most nearly whole waves; 32 otherwise). */
 APPFIS_GB_API int appfis_gb_star_r4(void* a, void* b, int dtype, int nx, int ny, int nz, int pitch, int iters, int mode,
                                     float coeff, const float* weights, int tile, int zchunk, int* cur_index,
                                     void* stream);
