@@ -236,6 +236,18 @@ namespace APPFIS
 		detail::AfterSweep(config);
 	}
 
+	// The reference's overlapped executors (Appfis/Runtime.hpp:372-594: boundary strips first, the
+	// halo exchange behind the interior) do the same sweep; with one rank per GPU there is no
+	// exchange to hide, so they are the plain executors.
+	template<typename T, typename... TArgs>
+	void ExecuteOverlap1D(Config<T>& config, TArgs... args) { Execute1D(config, args...); }
+
+	template<typename T, typename... TArgs>
+	void ExecuteOverlap2D(Config<T>& config, TArgs... args) { Execute2D(config, args...); }
+
+	template<typename T, typename... TArgs>
+	void ExecuteOverlap3D(Config<T>& config, TArgs... args) { Execute3D(config, args...); }
+
 	namespace detail
 	{
 		template<typename T>

@@ -216,7 +216,13 @@ static int RunGol(int argc, char** argv)
 	APPFIS::InitializeExecution(g);
 	APPFIS::Timer timer;
 	timer.Start("COMPUTE");
-	for (int t = 0; t < gens; t++) APPFIS::Execute2D(config, g.GetSubGrid(), g.GetSubGridNext());
+	for (int t = 0; t < gens; t++)  // the overlapped executor is the same sweep: alternate the two
+	{
+		if (t & 1)
+			APPFIS::ExecuteOverlap2D(config, g.GetSubGrid(), g.GetSubGridNext());
+		else
+			APPFIS::Execute2D(config, g.GetSubGrid(), g.GetSubGridNext());
+	}
 	timer.Stop("COMPUTE");
 	int live = 0;
 	APPFIS::Execute2DReduce(config, live, APPFIS::SUM, g);
