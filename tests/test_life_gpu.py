@@ -53,8 +53,10 @@ def test_golden(gb, torch_cuda, f):
         assert np.array_equal(out, g["out"]) and pop == int(g["live"])
 
 
+# nx a multiple of 16 runs the bulk-staged sweep: one strip narrower than 4096 cells (16, 48, 512,
+# 1040), exactly one strip (4096), a second strip of 16 cells (4112) and of 512 cells (8704)
 @pytest.mark.parametrize("nx,ny,gens", [(37, 29, 7), (1, 5, 3), (5, 1, 4), (16, 16, 9), (512, 48, 13), (1040, 70, 6),
-                                        (4096, 65, 5), (48, 131, 12)])
+                                        (4096, 65, 5), (48, 131, 12), (4112, 33, 9), (8704, 40, 4)])
 @pytest.mark.parametrize("rule", [0, 1])
 def test_u8_vs_oracle(gb, torch_cuda, nx, ny, gens, rule):
     cells = W.gol_cells(nx, ny, 0.35, nx * 7 + ny)
