@@ -650,7 +650,7 @@ int appfis_gb_life_job(const uint8_t* cells_in, uint8_t* cells_out, int nx, int 
     GB_CUDA(cudaMemcpyAsync(&pop, cnt, sizeof pop, cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
     if (population) *population = pop;
-    return APPFIS_GB_OK;
+    return gb::check_status("life_job");  // a bounded wait of the u8 sweep that gave up
 }
 
 }  // extern "C"
