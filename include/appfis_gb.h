@@ -112,7 +112,8 @@ APPFIS_GB_API int appfis_gb_ghost_periodic(void* field, int elem_size, int ndim,
  *   > 4, a dead cell is born when the count is 3, and otherwise the output buffer is left as it
  *   was (it then holds the state of two generations back).  Both buffers are read.
  * rule APPFIS_GB_LIFE_B3S23: Conway's B3/S23, a different function (not the reference's).
- * a = state at t, b = state at t-1 (zeros for the first call, as the reference zero-fills). */
+ * a = state at t, b = state at t-1 (zeros for the first call, as the reference zero-fills).
+ * With nx a multiple of 16 both buffers must be 16-byte aligned (rows are bulk-copied). */
 #define APPFIS_GB_LIFE_REFERENCE 0
 #define APPFIS_GB_LIFE_B3S23 1
 APPFIS_GB_API int appfis_gb_life_u8(uint8_t* a, uint8_t* b, int nx, int ny, int gens, int rule, int* cur_index, void* stream);
