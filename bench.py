@@ -64,9 +64,11 @@ def peaks():
 
 # ----------------------------------------------------------------------------- clocks
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during a timed region."""
+    """nvidia-smi clock / throttle sampling (every 50 ms) around a timed region; the summary keeps
+    the samples whose timestamps fall inside the region (mark_start / mark_end), and all samples
+    only if none does."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
@@ -74,22 +76,29 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.path = None
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
-        time.sleep(0.3)
+        time.sleep(0.3)  # nvidia-smi start-up
         return self
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
 
     def __exit__(self, *a):
         if self.proc is not None:
-            time.sleep(0.25)
+            time.sleep(0.1)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -97,12 +106,13 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        import datetime
         rows = []
         try:
             with open(self.path) as f:
                 for line in f:
                     parts = [x.strip() for x in line.split(",")]
-                    if len(parts) >= 9:
+                    if len(parts) >= 10:
                         rows.append(parts)
             os.unlink(self.path)
         except OSError:
@@ -116,12 +126,21 @@ class ClockSampler:
             except ValueError:
                 return None
 
-        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
-        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        def stamp(x):
+            try:
+                return datetime.datetime.strptime(x, "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                return None
+
+        inside = [r for r in rows if self.t0 is not None and stamp(r[0]) is not None
+                  and self.t0 - 0.05 <= stamp(r[0]) <= self.t1 + 0.05]
+        use = inside or rows
+        sm = [num(r[2]) for r in use if num(r[2]) is not None]
+        mx = [num(r[3]) for r in use if num(r[3]) is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        reasons = sorted({names[k] for r in use for k in range(4) if r[6 + k].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(use), "samples_in_timed_region": len(inside)}
 
 
 # ----------------------------------------------------------------------------- distributed
@@ -359,12 +378,14 @@ def run_ours(args, rank, world, local):
         sampler = ClockSampler(local) if sample_clocks else None
         if sampler:
             sampler.__enter__()
+            sampler.mark_start()
         e0.record(stream)
         for _ in range(k):
             step()
         e1.record(stream)
         torch.cuda.synchronize(dev)
         if sampler:
+            sampler.mark_end()
             sampler.__exit__()
         barrier(world)
         ms = max_over_ranks(e0.elapsed_time(e1), world) / k
