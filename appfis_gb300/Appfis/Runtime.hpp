@@ -10,7 +10,9 @@
  *     so Get/Set do no dependent load of a dims pointer; when all array arguments share one
  *     shape (checked on the host per launch) the views are rebuilt from a single copy of it,
  *     so a point's linear index is formed once for all arrays (Himeno's 14 arrays: 66 -> 77
- *     GLUP/s on GB300, the radius-4 star 139 -> 147);
+ *     GLUP/s on GB300, the radius-4 star 139 -> 147); boxes whose rows are not a multiple of 32
+ *     wide number the points of each (x, y) plane consecutively, so warps do not straddle a
+ *     mostly idle row end (Himeno's 129-wide rows: 77 -> 88);
  *   - blocks are 32 wide in x (coalesced rows) for every dimensionality;
  *   - after the sweep, the grids named by GridsToUpdate get their periodic ghosts refreshed on
  *     the device (no pack / host copy / MPI round trip) and are swapped; with one rank and no
@@ -189,6 +191,60 @@ namespace APPFIS
 			for (int k = kb; k < kb + M && k < z1; k++) STENCIL(i, j, k, HolderU<A>(args, s).get()...);
 		}
 
+		// Division by a launch-constant d > 0 as a multiply and shift: q = (n * m) >> k with
+		// k = 31 + ceil(log2 d), m = ceil(2^k / d), exact for every n < 2^31 (the error term
+		// n * (m*d - 2^k) stays below 2^k), and n * m < 2^64.
+		struct Div
+		{
+			unsigned long long m;
+			int k, d;
+		};
+
+		inline Div MakeDiv(int d)
+		{
+			int l = 0;
+			while ((1u << l) < (unsigned)d) l++;
+			Div v;
+			v.d = d;
+			v.k = 31 + l;
+			v.m = ((1ull << v.k) + (unsigned long long)d - 1) / (unsigned long long)d;
+			return v;
+		}
+
+		__device__ __forceinline__ unsigned DivQ(unsigned n, const Div& v) { return (unsigned)(((unsigned long long)n * v.m) >> v.k); }
+
+		// Box rows whose width is not a multiple of 32 leave the last warp of every row mostly
+		// idle in the 32-wide blocks; these kernels number the points of an (x, y) plane (rows
+		// of M points in y for the 2-D march) consecutively instead, so every warp but the
+		// plane's last is full.  Uniform shapes only.
+		template<int M, class... A>
+		__global__ void Functor2DF(int x0, int y0, int y1, unsigned n, Div w, Shape s, A... args)
+		{
+			const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
+			if (idx >= n) return;
+			const unsigned q = DivQ(idx, w);
+			const int i = x0 + (int)(idx - q * (unsigned)w.d), jb = y0 + (int)q * M;
+			for (int j = jb; j < jb + M && j < y1; j++) STENCIL(i, j, HolderU<A>(args, s).get()...);
+		}
+
+		template<int M, class... A>
+		__global__ void Functor3DF(int x0, int y0, int z0, int z1, unsigned n, Div w, Shape s, A... args)
+		{
+			const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
+			if (idx >= n) return;
+			const unsigned q = DivQ(idx, w);
+			const int i = x0 + (int)(idx - q * (unsigned)w.d), j = y0 + (int)q;
+			const int kb = z0 + (int)blockIdx.y * M;
+			for (int k = kb; k < kb + M && k < z1; k++) STENCIL(i, j, k, HolderU<A>(args, s).get()...);
+		}
+
+		// The flattened launch applies: ragged rows, the plane's points numbered below 2^31 and
+		// the z chunks within the grid's y limit.
+		inline bool Flatten(int w, long long plane, long long zchunks)
+		{
+			return w % 32 != 0 && plane < (1ll << 31) - 256 && zchunks <= 65535;
+		}
+
 		template<int M, class... A>
 		__global__ void Functor2D(int x0, int x1, int y0, int y1, A... args)
 		{
@@ -288,7 +344,12 @@ namespace APPFIS
 				detail::ArrayCount<typename detail::KArg<TArgs>::type...>::value <= detail::MARCH_MAX_ARRAYS ? detail::MARCH : 1;
 			dim3 blk(32, 8), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 8 * M));
 			detail::Shape s;
-			if (detail::UniformShape(s, args...))
+			const bool uniform = detail::UniformShape(s, args...);
+			const long long rows = (y1 - y0 + M - 1) / M, n = (long long)(x1 - x0) * rows;
+			if (uniform && detail::Flatten(x1 - x0, n, 1))
+				detail::Functor2DF<M, typename detail::KArg<TArgs>::type...><<<detail::Blocks((int)n, 256), 256, 0, GetCudaStream()>>>(
+					x0, y0, y1, (unsigned)n, detail::MakeDiv(x1 - x0), s, detail::KArg<TArgs>::to(args)...);
+			else if (uniform)
 				detail::Functor2DU<M, typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
 					x0, x1, y0, y1, s, detail::KArg<TArgs>::to(args)...);
 			else
@@ -307,10 +368,15 @@ namespace APPFIS
 		{
 			detail::Shape s;
 			const bool uniform = detail::UniformShape(s, args...);
+			const long long plane = (long long)(x1 - x0) * (y1 - y0);
 			if (detail::ArrayCount<typename detail::KArg<TArgs>::type...>::value <= detail::MARCH_MAX_ARRAYS)
 			{
 				dim3 blk(32, 8, 1), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 8), detail::Blocks(z1 - z0, detail::MARCH));
-				if (uniform)
+				if (uniform && detail::Flatten(x1 - x0, plane, grd.z))
+					detail::Functor3DF<detail::MARCH, typename detail::KArg<TArgs>::type...>
+						<<<dim3(detail::Blocks((int)plane, 256), grd.z), 256, 0, GetCudaStream()>>>(
+							x0, y0, z0, z1, (unsigned)plane, detail::MakeDiv(x1 - x0), s, detail::KArg<TArgs>::to(args)...);
+				else if (uniform)
 					detail::Functor3DU<detail::MARCH, typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
 						x0, x1, y0, y1, z0, z1, s, detail::KArg<TArgs>::to(args)...);
 				else
@@ -320,7 +386,11 @@ namespace APPFIS
 			else
 			{
 				dim3 blk(32, 4, 2), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 4), detail::Blocks(z1 - z0, 2));
-				if (uniform)
+				if (uniform && detail::Flatten(x1 - x0, plane, z1 - z0))
+					detail::Functor3DF<1, typename detail::KArg<TArgs>::type...>
+						<<<dim3(detail::Blocks((int)plane, 256), z1 - z0), 256, 0, GetCudaStream()>>>(
+							x0, y0, z0, z1, (unsigned)plane, detail::MakeDiv(x1 - x0), s, detail::KArg<TArgs>::to(args)...);
+				else if (uniform)
 					detail::Functor3DU<1, typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
 						x0, x1, y0, y1, z0, z1, s, detail::KArg<TArgs>::to(args)...);
 				else
