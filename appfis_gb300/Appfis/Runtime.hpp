@@ -211,7 +211,7 @@ namespace APPFIS
 			return v;
 		}
 
-		__device__ __forceinline__ unsigned DivQ(unsigned n, const Div& v) { return (unsigned)(((unsigned long long)n * v.m) >> v.k); }
+		__host__ __device__ __forceinline__ unsigned DivQ(unsigned n, const Div& v) { return (unsigned)(((unsigned long long)n * v.m) >> v.k); }
 
 		// Box rows whose width is not a multiple of 32 leave the last warp of every row mostly
 		// idle in the 32-wide blocks; these kernels number the points of an (x, y) plane (rows
