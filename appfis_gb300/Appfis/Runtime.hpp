@@ -11,8 +11,9 @@
  *     shape (checked on the host per launch) the views are rebuilt from a single copy of it,
  *     so a point's linear index is formed once for all arrays (Himeno's 14 arrays: 66 -> 77
  *     GLUP/s on GB300, the radius-4 star 139 -> 147); boxes whose rows are not a multiple of 32
- *     wide number the points of each (x, y) plane consecutively, so warps do not straddle a
- *     mostly idle row end (Himeno's 129-wide rows: 77 -> 88);
+ *     wide, and launches without the march below, number the points of each (x, y) plane
+ *     consecutively, so warps do not straddle a mostly idle row end (Himeno's 129-wide rows:
+ *     77 -> 88; Triton's FP64 functors 2.72 -> 3.14 with the 2-D march limited to two arrays);
  *   - blocks are 32 wide in x (coalesced rows) for every dimensionality;
  *   - after the sweep, the grids named by GridsToUpdate get their periodic ghosts refreshed on
  *     the device (no pack / host copy / MPI round trip) and are swapped; with one rank and no
@@ -104,7 +105,9 @@ namespace APPFIS
 		// pays only for functors over a few fields (measured on GB300: the radius-4 star over 2
 		// arrays 107 -> 139 GLUP/s; Himeno over 14 arrays 68 -> 48, its loads in flight are what
 		// count), so functors taking more than MARCH_MAX_ARRAYS arrays keep one point per thread.
-		constexpr int MARCH = 4, MARCH_MAX_ARRAYS = 4;
+		// In 2-D the march pays only for functors over one or two fields (GameOfLife); Triton's
+		// pointwise dt and 5-point wet/dry functors over 4 arrays ran 8% faster without it.
+		constexpr int MARCH = 4, MARCH_MAX_ARRAYS = 4, MARCH_MAX_ARRAYS_2D = 2;
 
 		template<class A> struct IsArrayArg { static const int value = 0; };
 		template<class U> struct IsArrayArg<ArrayArg<U> > { static const int value = 1; };
@@ -216,7 +219,11 @@ namespace APPFIS
 		// Box rows whose width is not a multiple of 32 leave the last warp of every row mostly
 		// idle in the 32-wide blocks; these kernels number the points of an (x, y) plane (rows
 		// of M points in y for the 2-D march) consecutively instead, so every warp but the
-		// plane's last is full.  Uniform shapes only.
+		// plane's last is full.  Uniform shapes only.  Launches without the march take this
+		// form at every width too: a CTA then covers 256 consecutive points of one row instead
+		// of 8 rows of 32 (Triton's FP64 functors over 8-11 arrays: 2.94 -> 3.14 GLUP/s); with
+		// the march the 32 x 8 blocks stay faster where the rows are whole warps (GameOfLife
+		// 319 against 308, the radius-4 star 146 against 142).
 		template<int M, class... A>
 		__global__ void Functor2DF(int x0, int y0, int y1, unsigned n, Div w, Shape s, A... args)
 		{
@@ -238,11 +245,11 @@ namespace APPFIS
 			for (int k = kb; k < kb + M && k < z1; k++) STENCIL(i, j, k, HolderU<A>(args, s).get()...);
 		}
 
-		// The flattened launch applies: ragged rows, the plane's points numbered below 2^31 and
-		// the z chunks within the grid's y limit.
-		inline bool Flatten(int w, long long plane, long long zchunks)
+		// The flattened launch applies: ragged rows or no march (M == 1), the plane's points
+		// numbered below 2^31 and the z chunks within the grid's y limit.
+		inline bool Flatten(int w, int M, long long plane, long long zchunks)
 		{
-			return w % 32 != 0 && plane < (1ll << 31) - 256 && zchunks <= 65535;
+			return (w % 32 != 0 || M == 1) && plane < (1ll << 31) - 256 && zchunks <= 65535;
 		}
 
 		template<int M, class... A>
@@ -341,12 +348,12 @@ namespace APPFIS
 		if (x1 > x0 && y1 > y0)
 		{
 			constexpr int M =
-				detail::ArrayCount<typename detail::KArg<TArgs>::type...>::value <= detail::MARCH_MAX_ARRAYS ? detail::MARCH : 1;
+				detail::ArrayCount<typename detail::KArg<TArgs>::type...>::value <= detail::MARCH_MAX_ARRAYS_2D ? detail::MARCH : 1;
 			dim3 blk(32, 8), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 8 * M));
 			detail::Shape s;
 			const bool uniform = detail::UniformShape(s, args...);
 			const long long rows = (y1 - y0 + M - 1) / M, n = (long long)(x1 - x0) * rows;
-			if (uniform && detail::Flatten(x1 - x0, n, 1))
+			if (uniform && detail::Flatten(x1 - x0, M, n, 1))
 				detail::Functor2DF<M, typename detail::KArg<TArgs>::type...><<<detail::Blocks((int)n, 256), 256, 0, GetCudaStream()>>>(
 					x0, y0, y1, (unsigned)n, detail::MakeDiv(x1 - x0), s, detail::KArg<TArgs>::to(args)...);
 			else if (uniform)
@@ -372,7 +379,7 @@ namespace APPFIS
 			if (detail::ArrayCount<typename detail::KArg<TArgs>::type...>::value <= detail::MARCH_MAX_ARRAYS)
 			{
 				dim3 blk(32, 8, 1), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 8), detail::Blocks(z1 - z0, detail::MARCH));
-				if (uniform && detail::Flatten(x1 - x0, plane, grd.z))
+				if (uniform && detail::Flatten(x1 - x0, detail::MARCH, plane, grd.z))
 					detail::Functor3DF<detail::MARCH, typename detail::KArg<TArgs>::type...>
 						<<<dim3(detail::Blocks((int)plane, 256), grd.z), 256, 0, GetCudaStream()>>>(
 							x0, y0, z0, z1, (unsigned)plane, detail::MakeDiv(x1 - x0), s, detail::KArg<TArgs>::to(args)...);
@@ -386,7 +393,7 @@ namespace APPFIS
 			else
 			{
 				dim3 blk(32, 4, 2), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 4), detail::Blocks(z1 - z0, 2));
-				if (uniform && detail::Flatten(x1 - x0, plane, z1 - z0))
+				if (uniform && detail::Flatten(x1 - x0, 1, plane, z1 - z0))
 					detail::Functor3DF<1, typename detail::KArg<TArgs>::type...>
 						<<<dim3(detail::Blocks((int)plane, 256), z1 - z0), 256, 0, GetCudaStream()>>>(
 							x0, y0, z0, z1, (unsigned)plane, detail::MakeDiv(x1 - x0), s, detail::KArg<TArgs>::to(args)...);
