@@ -436,9 +436,25 @@ namespace APPFIS
 			const int box[6] = { config.GetStartX(), config.GetEndX(),
 				nDim > 1 ? config.GetStartY() : 0, nDim > 1 ? config.GetEndY() : 1,
 				nDim > 2 ? config.GetStartZ() : 0, nDim > 2 ? config.GetEndZ() : 1 };
+			const int py = a->GetDimCount() > 1 ? a->GetDim(1) : 1;
+			if (DType<T>::code == APPFIS_GB_I32)
+			{
+				// The reference accumulates an int reduction in int (Runtime.hpp:597-913), so a SUM
+				// outside the int range wraps there.  The engine sums in int64; its low 32 bits are
+				// that wrapped total, taken here with a defined narrowing (no double round trip).
+				static long long* dres = nullptr;
+				if (!dres) CheckCuda(cudaMalloc((void**)&dres, sizeof(long long)), "cudaMalloc(reduction result)");
+				Check(appfis_gb_reduce(grid.DeviceCurrent(), DType<T>::code, a->GetDim(0), py, box, (int)rType, dres,
+					GetCudaStream()), "reduction");
+				long long v = 0;
+				CheckCuda(cudaMemcpyAsync(&v, dres, sizeof v, cudaMemcpyDeviceToHost, GetCudaStream()), "reduction result copy");
+				CheckCuda(cudaStreamSynchronize(GetCudaStream()), "reduction");
+				var = (T)static_cast<int>(static_cast<uint32_t>(static_cast<unsigned long long>(v)));
+				return;
+			}
 			double r = 0.0;
-			Check(appfis_gb_reduce_host(grid.DeviceCurrent(), DType<T>::code, a->GetDim(0), a->GetDimCount() > 1 ? a->GetDim(1) : 1,
-				box, (int)rType, &r, GetCudaStream()), "reduction");
+			Check(appfis_gb_reduce_host(grid.DeviceCurrent(), DType<T>::code, a->GetDim(0), py, box, (int)rType, &r,
+				GetCudaStream()), "reduction");
 			var = (T)r;
 		}
 	}

@@ -124,15 +124,15 @@ int launch_reduce(const void* field, int px, int py, const int* b, int op, void*
 }
 
 // ---------------------------------------------------------------- allocation-free variant
-// Some callers cannot allocate device memory at the moment they need a reduction: code that
-// runs while a stream is being captured into a CUDA graph (an allocation there fails or breaks
-// the capture), code inside a host framework whose allocator has reserved all device memory,
-// or a latency-critical loop where the synchronising cudaMalloc/cudaFree of a first call is not
-// acceptable.  For them the same reduction kernel can take its scratch (one ticket counter and
-// one partial per block) from a fixed array that is part of the library image instead of the
-// grow-only workspace.  64 KiB holds the ticket and 8160 partials; the kernel uses at most
-// 4 blocks per SM (608 on a GB300), so every box fits on current GPUs.  Every device that loads
-// the library keeps this array until the process exits.
+// Some callers cannot allocate device memory at the moment they need a reduction: a host
+// framework whose caching allocator has reserved the device memory, a library embedded in a
+// runtime that owns every allocation, or a latency-critical loop that cannot take the implicit
+// synchronisation of a first cudaMalloc/cudaFree.  For them the same reduction kernel can take
+// its scratch (one ticket counter and one partial per block) from a fixed array that is part of
+// the library image instead of the grow-only workspace.  64 KiB holds the ticket and 8160
+// partials; the kernel uses at most 4 blocks per SM (608 on a GB300), so every box fits on
+// current GPUs.  Every device that loads the library keeps this array until the process exits
+// (under lazy module loading the runtime commits it on the first use of the module on a device).
 constexpr size_t NOALLOC_SCRATCH_BYTES = 64 * 1024;
 constexpr size_t NOALLOC_MAX_PARTIALS = (NOALLOC_SCRATCH_BYTES - 256) / sizeof(double);
 static __device__ __align__(256) unsigned char g_reduce_scratch[NOALLOC_SCRATCH_BYTES];

@@ -77,17 +77,24 @@ APPFIS_GB_API int appfis_gb_stream_sync(void* stream);
  * (fixed-order tree: per-block partials, then the last block folds them in block order). */
 APPFIS_GB_API int appfis_gb_reduce(const void* field, int dtype, int px, int py, const int* box, int op, void* dev_result,
                      void* stream);
-/* Same reduction, same result, for callers that must not allocate device memory — e.g. code
- * running while a stream is captured into a CUDA graph, inside a framework whose allocator has
- * reserved the device memory, or in a loop that cannot afford a synchronising cudaMalloc.  No
- * counterpart in the reference (its reductions allocate nothing beyond the grid's own buffers).
+/* Same reduction, same result, for callers that must not allocate device memory: a host
+ * framework whose caching allocator has already reserved the device memory (a cudaMalloc there
+ * fails, or fragments the framework's pool), a library embedded in another runtime that owns
+ * every allocation, or a latency-critical loop where the implicit device synchronisation of a
+ * first cudaMalloc/cudaFree would stall the pipeline.  No counterpart in the reference (its
+ * reductions allocate nothing beyond the grid's own buffers).
  * The scratch (a ticket and one partial sum per block) lives in a fixed 64 KiB device array
  * inside the library, held by every device that loads it until the process exits; a box whose
  * reduction needs more than 8160 partial sums is rejected with APPFIS_GB_EINVAL (this kernel
- * uses at most 4 per SM).  Nothing is allocated: the first call on a device looks up the array's
- * device address with that device current (make that first call before any stream capture);
- * every call clears the ticket with an asynchronous memset on `stream`.  All calls share the
- * array, so calls that overlap on the GPU (other streams, other host threads) race: order them. */
+ * uses at most 4 per SM).  The entry point calls no cudaMalloc, cudaFree or allocating library
+ * routine.  Set-up: the first call on a device, with that device current, looks up the array's
+ * device address (cudaGetSymbolAddress) and caches it; make that first call before any stream
+ * capture.  Under CUDA's default lazy module loading the runtime commits the array's 64 KiB and
+ * loads each (dtype, op) kernel instance on first use, so warm up every dtype/op pair you will
+ * use before the device memory is handed to another allocator (or set CUDA_MODULE_LOADING=EAGER,
+ * which loads everything when the library's module is first used).  Every call clears the
+ * ticket with an asynchronous memset on `stream`.  All calls share the array, so calls that
+ * overlap on the GPU (other streams, other host threads) race: order them. */
 APPFIS_GB_API int appfis_gb_reduce_noalloc(const void* field, int dtype, int px, int py, const int* box, int op,
                                            void* dev_result, void* stream);
 /* Same, returning the value on the host (synchronises `stream`). */
@@ -144,7 +151,7 @@ APPFIS_GB_API int appfis_gb_life_job(const uint8_t* cells_in, uint8_t* cells_out
  * per launch in shared memory) with the identical per-point arithmetic. */
 APPFIS_GB_API int appfis_gb_heat2d(float* a, float* b, int nx, int ny, int pitch, int iters, float cx, float cy, int* cur_index,
                      void* stream);
-/* One sweep per launch (the plain form; also what the drop-in Execute2D registration uses). */
+/* One sweep per launch (the plain form). */
 APPFIS_GB_API int appfis_gb_heat2d_sweep(const float* cur, float* next, int nx, int ny, int pitch, float cx, float cy, void* stream);
 /* Whole run from host: field is the padded (nx+2)*(ny+2) dense array (ghost ring included), in
  * place.  stats (optional, 3 doubles): MAX, MIN, SUM of the interior at the end (reference seeds). */

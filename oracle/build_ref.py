@@ -7,7 +7,8 @@ MPI stand-in in mpi_stub/.  Outputs go to oracle/_ref/ only (git-ignored).
 Two stages, so that the same reference code can also run on a machine that has no copy of
 the reference sources:
 
-1. Where the reference tree is present (REF_ROOT, default /root/reference), each harness
+1. Where the reference tree is present (REF_ROOT: $APPFIS_REF_ROOT, else a checkout named
+   `reference` beside this repository), each harness
    TU is flattened into oracle/_ref/ref_<name>.flat.cpp: every quoted #include that
    resolves (the harness helper, the reference's app header, Appfis/*.hpp, the MPI
    stand-in) is inlined in place, system <...> includes are kept.  Nothing of it is
@@ -27,7 +28,7 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_ROOT = os.environ.get("APPFIS_REF_ROOT", "/root/reference")
+REF_ROOT = os.environ.get("APPFIS_REF_ROOT") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 HARNESSES = ["gol", "heat2d", "himeno", "fdtd", "triton"]
 INC_RE = re.compile(r'^\s*#\s*include\s+"([^"]+)"')
 

@@ -10,6 +10,7 @@
 //        dropin_runner himeno NX NY NZ ITERS OMEGA coef.f32 p.f32 out.f32
 //        dropin_runner fdtd   NX NY NZ ITERS COEFF in.f32 out.f32
 //        dropin_runner triton NX NY DX CN HEXTRA MANN T_END PRINT TSTEP MAXSTEPS dem.f64 h.f64 out.f64 dt.f64
+//        dropin_runner ireduce NX NY in.i32           (Execute2DReduce SUM / MAX / MIN of an int grid)
 #include <cfloat>
 #include <cstdio>
 #include <cstdlib>
@@ -402,6 +403,31 @@ static int RunTriton(int argc, char** argv)
 	return 0;
 }
 
+// int reductions: the reference accumulates in int, so a SUM outside the int range wraps
+static int RunIntReduce(int argc, char** argv)
+{
+	const int nx = std::atoi(argv[2]), ny = std::atoi(argv[3]);
+	std::vector<char> in = ReadFile(argv[4], sizeof(int) * (size_t)nx * ny);
+	const int* src = reinterpret_cast<const int*>(in.data());
+	APPFIS::Attribute attr;
+	APPFIS::Initialize(argc, argv, APPFIS::DIM_2D, APPFIS::DIM_2D, attr);
+	APPFIS::Grid<int> g(APPFIS::DIM_2D, nx, ny, APPFIS::SINGLE);
+	g.AllocateFullGrid();
+	for (int j = 0; j < ny; j++)
+		for (int i = 0; i < nx; i++) g.GetFullGrid()->Set(i, j, src[(size_t)j * nx + i]);
+	APPFIS::Scatter(g.GetFullGrid(), g.GetSubGrid());
+	APPFIS::Config<int> config(g);
+	APPFIS::InitializeExecution(g);
+	int sm = 0, mx = 0, mn = 0;
+	APPFIS::Execute2DReduce(config, sm, APPFIS::SUM, g);
+	APPFIS::Execute2DReduce(config, mx, APPFIS::MAX, g);
+	APPFIS::Execute2DReduce(config, mn, APPFIS::MIN, g);
+	APPFIS::FinalizeExecution(g);
+	std::printf("{\"sum\": %d, \"max\": %d, \"min\": %d}\n", sm, mx, mn);
+	APPFIS::Finalize();
+	return 0;
+}
+
 int main(int argc, char** argv)
 {
 	if (argc < 2) return 2;
@@ -411,6 +437,7 @@ int main(int argc, char** argv)
 	if (mode == "himeno") return RunHimeno(argc, argv);
 	if (mode == "fdtd") return RunFdtd(argc, argv);
 	if (mode == "triton") return RunTriton(argc, argv);
+	if (mode == "ireduce") return RunIntReduce(argc, argv);
 	std::fprintf(stderr, "unknown mode %s\n", argv[1]);
 	return 2;
 }

@@ -11,8 +11,9 @@ from concurrent.futures import ThreadPoolExecutor
 
 import pytest
 
-REF = os.environ.get("APPFIS_REF_ROOT", "/root/reference")
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+# the reference checkout: $APPFIS_REF_ROOT, else a directory named `reference` beside this repository
+REF = os.environ.get("APPFIS_REF_ROOT") or os.path.normpath(os.path.join(ROOT, "..", "reference"))
 APPS = ["HeatDiffusion", "GameOfLife", "Himeno", "FDTD3d", "Triton"]
 
 

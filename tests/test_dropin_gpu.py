@@ -99,3 +99,17 @@ def test_triton_golden(runner, f):
     np.testing.assert_allclose(out[:n].reshape(ny, nx), g["h"], atol=1e-9)
     np.testing.assert_allclose(out[n:2 * n].reshape(ny, nx), g["qx"], atol=1e-9)
     np.testing.assert_allclose(out[2 * n:].reshape(ny, nx), g["qy"], atol=1e-9)
+
+
+@pytest.mark.parametrize("lo,hi", [(-1000, 1000), (1 << 29, (1 << 31) - 1), (-(1 << 31), -(1 << 29))])
+def test_int_reduce_wraps_like_int(runner, lo, hi):
+    """Execute2DReduce on an int grid: MAX / MIN exact, SUM equal to the reference's int
+    accumulation (wrapped modulo 2^32 when the total leaves the int range)."""
+    rng = np.random.default_rng(lo & 0xffff)
+    nx, ny = 301, 77
+    a = rng.integers(lo, hi, size=(ny, nx), dtype=np.int64).astype(np.int32)
+    res, _ = run(runner, ["ireduce", nx, ny, "{in0}"], [a], [])
+    total = int(a.astype(np.int64).sum())
+    wrapped = (total + (1 << 31)) % (1 << 32) - (1 << 31)
+    assert res["sum"] == wrapped
+    assert res["max"] == int(a.max()) and res["min"] == int(a.min())

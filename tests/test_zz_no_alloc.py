@@ -1,17 +1,20 @@
 """The allocation-free reduction entry point, for callers that cannot allocate device memory
-when they reduce (inside a graph capture, under a framework allocator that holds the device
-memory, or where a first-call cudaMalloc would stall a latency-critical loop).
+when they reduce (under a framework allocator that holds the device memory, inside a runtime
+that owns every allocation, or where a first-call cudaMalloc would stall a latency-critical
+loop).
 
 appfis_gb_reduce_noalloc is called through the C ABI and must give what appfis_gb_reduce gives
 on the same field — MAX and MIN exactly, SUM within the 1e-12 relative tolerance of the other
 reduction tests — on two calls in a row (the second one reuses the fixed scratch left by the
-first).  This file runs last so that a failure here cannot hide any other test."""
+first); the oracle's value is checked as well.  This file runs last so that a failure here
+cannot hide any other test."""
 import ctypes
 
 import numpy as np
 import pytest
 
 from appfis_gb300 import workloads as W
+from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -44,3 +47,6 @@ def test_noalloc_matches_workspace_reduction(gb, torch_cuda, dtype, code, shape,
                 assert abs(g - w) <= 1e-12 * max(1.0, abs(w)), (op, call, g, w)
             else:
                 assert g == w, (op, call, g, w)
+        o = O.reduce(a if len(shape) == 3 else a[None], list(box) + ([0, 1] if len(box) == 4 else []),
+                     ("max", "min", "sum")[op])
+        assert abs(got.item() - o) <= 1e-12 * max(1.0, abs(o)), (op, got.item(), o)
