@@ -46,6 +46,9 @@ SIGNATURES = {
     "appfis_gb_himeno_mixed": [_P, _P, _P, _P, _i, _i, _i, _i, _i, _i, _f, _P, _P, _P],
     "appfis_gb_himeno_job": [_P, _P, _i, _i, _i, _i, _f, _i, _i, _P],
     "appfis_gb_star_r4": [_P, _P, _i, _i, _i, _i, _i, _i, _i, _f, _P, _i, _i, _P, _P],
+    "appfis_gb_heat2d_f64": [_P, _P, _i, _i, _i, _i, _d, _d, _P, _P],
+    "appfis_gb_himeno_f64": [_P, _P, _P, _i, _i, _i, _i, _i, _d, _P, _P, _P],
+    "appfis_gb_star_r4_f64": [_P, _P, _i, _i, _i, _i, _i, _i, _d, _P, _P, _P],
     "appfis_gb_flood_run": [_P, _i, _i, _P, _P, _P, _P, _P, _P],
     "appfis_gb_flood_setup": [_P, _i, _P, _P, _P, _P, _d, _P],
     "appfis_gb_flood_job": [_i, _P, _P, _P, _P, _P, _P, _d, _P, _i, _P, _P, _P],

@@ -470,9 +470,13 @@ int run_u8(uint8_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStream
     return APPFIS_GB_OK;
 }
 
-// Time-blocked launches for whole blocks of TB_STEPS generations (ping-pong between (a, b) and
-// two workspace planes), single-generation sweeps for the remainder.  The newest state ends in
-// a or b as cur_index says.
+// Time-blocked launches for whole blocks of TB_STEPS generations, single-generation sweeps for
+// the remainder.  A launch reads a (cur, old) pair and writes another pair (its tiles read
+// neighbours' halo rows, so it cannot write in place).  An even number of launches ping-pongs
+// between (a, b) and a workspace pair; an odd number of three or more first goes round three
+// pairs once ((a, b) -> W1 -> W2 -> (a, b)) and then ping-pongs, so the newest state ends in
+// (a, b) without a copy; a single launch copies its pair back.  cur_index tells which of a, b
+// holds the newest state.
 template <int RULE>
 int run_bits(uint32_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStream_t st)
 {
@@ -480,10 +484,15 @@ int run_bits(uint32_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStr
     int ci = 0;
     const size_t plane = (size_t)nw * ny;
     if (gens >= TB_STEPS) {
-        void *wc, *wd;
+        const int launches = gens / TB_STEPS;
+        void *wc, *wd, *we = nullptr, *wf = nullptr;
         GB_TRY(gb::workspace(gb::WS_LIFE_C, sizeof(uint32_t) * plane, &wc));
         GB_TRY(gb::workspace(gb::WS_LIFE_D, sizeof(uint32_t) * plane, &wd));
-        uint32_t* P[2][2] = {{buf[0], buf[1]}, {(uint32_t*)wc, (uint32_t*)wd}};  // [pair][cur/old]
+        if (launches % 2 == 1 && launches >= 3) {
+            GB_TRY(gb::workspace(gb::WS_LIFE_E, sizeof(uint32_t) * plane, &we));
+            GB_TRY(gb::workspace(gb::WS_LIFE_F, sizeof(uint32_t) * plane, &wf));
+        }
+        uint32_t* P[3][2] = {{buf[0], buf[1]}, {(uint32_t*)wc, (uint32_t*)wd}, {(uint32_t*)we, (uint32_t*)wf}};  // [pair][cur/old]
         const int tiles_x = (nw + 29) / 30, tiles = tiles_x * ((ny + TB_ROWS - 1) / TB_ROWS);
         int per_sm = 0;
         const int tsm = 2 * TB_RR * 32 * 4;
@@ -493,18 +502,18 @@ int run_bits(uint32_t* buf[2], int nx, int ny, int gens, int* cur_index, cudaStr
             per_sm = 4;
         const int grid = std::max(1, std::min(tiles, per_sm * gb::sm_count()));
         int pair = 0;
-        int done = 0;
-        for (; done + TB_STEPS <= gens; done += TB_STEPS) {
-            life_bits_tb<RULE><<<grid, TB_WARPS * 32, tsm, st>>>(P[pair][0], P[pair][1], P[1 - pair][0], P[1 - pair][1], nw, ny,
-                                                               tiles_x, tiles, TB_STEPS);
-            pair = 1 - pair;
+        for (int n = 0; n < launches; n++) {
+            const int next = (we && n < 3) ? (n + 1) % 3 : 1 - pair;  // the three-pair round first, then ping-pong
+            life_bits_tb<RULE><<<grid, TB_WARPS * 32, tsm, st>>>(P[pair][0], P[pair][1], P[next][0], P[next][1], nw, ny, tiles_x,
+                                                               tiles, TB_STEPS);
+            pair = next;
         }
         GB_TRY(gb::launched("life_bits_tb"));
-        if (pair == 1) {  // bring the (cur, old) pair back into (a, b)
-            GB_CUDA(cudaMemcpyAsync(buf[0], P[1][0], sizeof(uint32_t) * plane, cudaMemcpyDeviceToDevice, st));
-            GB_CUDA(cudaMemcpyAsync(buf[1], P[1][1], sizeof(uint32_t) * plane, cudaMemcpyDeviceToDevice, st));
+        if (pair != 0) {  // one launch: bring the (cur, old) pair back into (a, b)
+            GB_CUDA(cudaMemcpyAsync(buf[0], P[pair][0], sizeof(uint32_t) * plane, cudaMemcpyDeviceToDevice, st));
+            GB_CUDA(cudaMemcpyAsync(buf[1], P[pair][1], sizeof(uint32_t) * plane, cudaMemcpyDeviceToDevice, st));
         }
-        gens -= done;
+        gens -= launches * TB_STEPS;
     }
     if (gens > 0) {
         const int strips = (nw + 31) / 32;

@@ -174,6 +174,16 @@ def max_over_ranks(x, world):
     return float(t.item())
 
 
+def reference_gol_record():
+    """The reference CPU path's result for this exact workload (population and a hash of the
+    final state), recorded by tests/golden/make_golden.py --full-gol; None when absent."""
+    p = os.path.join(ROOT, "tests", "golden", "gol_%dx%d_g%d.json" % (GOL_NX, GOL_NY, GOL_GENS))
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f)
+
+
 # ----------------------------------------------------------------------------- CPU baseline
 def cpu_gol_sample(cells, gens):
     """Reference OpenMP path (oracle/_ref/ref_gol) on the full grid for `gens` generations;
@@ -407,7 +417,7 @@ def run_ours(args, rank, world, local):
     population = int(cnt.item())
     value = N * gens / (ms_bits * 1e-3) / 1e9 * world
 
-    # dominant kernel alone: the bit-packed sweep, average launch duration over G launches
+    # dominant kernel alone: average launch duration over G launches issued from the stream
     def kernel_avg(fn_name, a, b, g):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -417,12 +427,26 @@ def run_ours(args, rank, world, local):
         torch.cuda.synchronize(dev)
         return e0.elapsed_time(e1) / g
 
-    # the dominant kernel is life_bits_tb: one launch advances the whole grid by TB_GENS generations;
-    # its algorithmic bytes are the compulsory per-sweep bytes (cur + old read, new written: 3 bits
-    # per cell) times the generations it covers, so time blocking can read above 1.0
+    # the dominant kernel is life_bits_tb: one launch advances the whole grid by TB_GENS
+    # generations.  Its launch time comes from a CUDA graph of TB_LAUNCHES back-to-back launches
+    # (no launch gaps, no copies: an odd launch count ends in (a, b) by itself), replayed 4 times.
+    TB_LAUNCHES = 25
     gb.call("appfis_gb_life_pack", d_cells.data_ptr(), wa.data_ptr(), GOL_NX, GOL_NY, sp)
-    kernel_avg("appfis_gb_life_bits", wa, wb, 20 * TB_GENS)
-    bits_ms = kernel_avg("appfis_gb_life_bits", wa, wb, 25 * TB_GENS) * TB_GENS  # per launch
+    wb.zero_()
+
+    def tb_launches():
+        gb.call("appfis_gb_life_bits", wa.data_ptr(), wb.data_ptr(), GOL_NX, GOL_NY, TB_LAUNCHES * TB_GENS, 0,
+                ctypes.byref(ci), torch.cuda.current_stream(dev).cuda_stream)
+
+    replay_tb = graph_of(torch, tb_launches)
+    bits_ms = _time(torch, stream, replay_tb, reps=4, warmup=2) / TB_LAUNCHES  # per launch
+    # its bound is the integer/logic pipe, not HBM: per word (32 cells) and generation the source
+    # issues 13 logic instructions (11 lop3 + 2 funnel shifts: the row summaries and the
+    # bit-sliced count and rule); the pipe retires 64 such lanes per SM and clock
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    word_gens = (N // 32) * TB_GENS
+    logic_ops = 13 * word_gens
+    ops_achieved = logic_ops / (bits_ms * 1e-3) / 1e12  # Tops/s
     bits_bytes = N * 3 / 8 * TB_GENS
     bits_achieved = bits_bytes / (bits_ms * 1e-3) / 1e9
 
@@ -452,7 +476,12 @@ def run_ours(args, rank, world, local):
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
     e2e_value = N * gens / e2e_s / 1e9 * world
     assert pop.value == population == pop_u8, "forms disagree on the population"
+    import hashlib
+    final_sha = hashlib.sha256(host_out.numpy().tobytes()).hexdigest()  # the e2e run's final grid
 
+    alu_mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz") or 2070.0
+    alu_peak = sms * 64 * alu_mhz * 1e6 / 1e12  # Tops/s
+    ref_gol = reference_gol_record()
     line = {
         "metric": METRIC, "value": value, "unit": "GLUP/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_bits, "higher_is_better": True, "scaling": "weak",
@@ -462,15 +491,27 @@ def run_ours(args, rank, world, local):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "each step starts from the 268 MB u8 grid (larger than L2); the packed state (67 MB for "
                          "both buffers) stays L2-resident across generations within a step",
-                   "population": population},
+                   "population": population,
+                   "population_equals_reference_cpu_path": (population == ref_gol["live"]) if ref_gol else None,
+                   "final_state_equals_reference_cpu_path": (final_sha == ref_gol["sha256"]) if ref_gol else None},
         "e2e": {"value": e2e_value, "unit": "GLUP/s", "h2d_bytes_per_step": N, "d2h_bytes_per_step": N + 8,
                 "ms_per_step": e2e_s * 1e3},
         "gpu_launches": args.steps * (gens // 16 + gens % 16 + 2),  # pack, time-blocked sweeps, remainder, population
-        "roofline": {"bound": "hbm", "achieved": bits_achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": bits_achieved / hbm_peak, "traffic": profiled_traffic("life_bits_tb"),
+        "roofline": {"bound": "alu", "achieved": ops_achieved, "peak": alu_peak, "unit": "Tops/s",
+                     "frac": ops_achieved / alu_peak, "traffic": profiled_traffic("life_bits_tb"),
                      "kernel": "life_bits_tb", "generations_per_launch": TB_GENS,
-                     "algorithmic_bytes_per_launch": bits_bytes, "avg_launch_ms": bits_ms,
-                     "peak_source": peak_kind},
+                     "ops": "32-bit integer logic instructions (lop3, funnel shift), per lane",
+                     "ops_per_word_generation": 13, "algorithmic_ops_per_launch": logic_ops,
+                     "avg_launch_ms": bits_ms, "launches_per_step": GOL_GENS // TB_GENS,
+                     "launch_timing": "CUDA graph of %d back-to-back launches" % TB_LAUNCHES,
+                     "peak_source": "%d SMs x 64 logic lanes per clock x %.0f MHz (median SM clock of the timed region)"
+                                    % (sms, alu_mhz),
+                     "hbm_effective": {"achieved_gbs": bits_achieved, "peak_gbs": hbm_peak,
+                                       "frac": bits_achieved / hbm_peak, "peak_source": peak_kind,
+                                       "algorithmic_bytes_per_launch": bits_bytes,
+                                       "note": "compulsory bytes of 16 one-generation sweeps (0.375 B per cell each); "
+                                               "the tile stays on chip for the 16 generations, so DRAM moves only "
+                                               "`traffic` per launch"}},
         "forms": {
             "bits": {"glups": value, "ms_per_step": ms_bits, "kernel_ms": bits_ms, "achieved_gbs": bits_achieved},
             "u8": {"glups": N * gens / (ms_u8 * 1e-3) / 1e9 * world, "ms_per_step": ms_u8, "kernel_ms": u8_ms,
@@ -548,6 +589,15 @@ def bench_heat(torch, gb, W, dev, sp, hbm):
 
     ms = _time(torch, sp, run)
     ms_g = _time(torch, sp, graph_of(torch, run))
+    a.copy_(f)
+    b.copy_(f)
+    run()
+    out32 = (a if ci.value == 0 else b).double()
+    f64 = f.double()
+    a64, b64 = f64.clone(), f64.clone()
+    gb.call("appfis_gb_heat2d_f64", a64.data_ptr(), b64.data_ptr(), nx, ny, nx + 2, it, float(c["r"]), float(c["r"]),
+            ctypes.byref(ci), sp.cuda_stream)
+    ref64 = a64 if ci.value == 0 else b64
     lups = nx * ny * it
     best = min(ms, ms_g)
     gbs = lups * 8 / (best * 1e-3) / 1e9
@@ -555,7 +605,17 @@ def bench_heat(torch, gb, W, dev, sp, hbm):
             "ms_stream_launches": ms, "ms_cuda_graph": ms_g, "bytes_per_lup": 8, "effective_gbs": gbs, "frac_of_hbm": gbs / hbm,
             "note": "8.4 MB working set is L2-resident; 8 sweeps per launch on chip (4x4 point blocks in registers, "
                     "block edges through shared memory; 125 launches, replayed from a CUDA graph); HBM fraction is nominal",
-            "form": "plain FP32 (bit-identical to the reference CPU path)"}
+            "form": "plain FP32 (bit-identical to the reference CPU path)",
+            "error_vs_fp64": _err(out32, ref64), "l2_norm": float(out32[1:-1, 1:-1].norm().item()),
+            "l2_norm_fp64": float(ref64[1:-1, 1:-1].norm().item())}
+
+
+def _err(x, ref):
+    """Error of a result against the FP64 result of the same workload: max |x - ref|, the
+    relative L2 error ||x - ref|| / ||ref|| and max |ref| (computed in double on the device)."""
+    d = x.double() - ref
+    return {"max_abs": float(d.abs().max().item()), "rel_l2": float((d.norm() / ref.norm().clamp_min(1e-300)).item()),
+            "ref_max_abs": float(ref.abs().max().item())}
 
 
 def _pad_x(t, pitch):
@@ -607,6 +667,25 @@ def bench_himeno(torch, gb, W, dev, sp, hbm):
                               gosa.data_ptr(), ctypes.byref(ci), sp.cuda_stream)
         return _time(torch, sp, one, reps=1) / n
 
+    # FP64 reference of the same 400 sweeps (appfis_gb_himeno_f64; dense 259-element rows)
+    coef64 = coef_d.double()
+    ptr64 = (ctypes.c_void_p * 12)(*[coef64[k].data_ptr() for k in range(12)])
+    q64a, q64b = p0_d.double(), torch.zeros_like(p0_d, dtype=torch.float64)
+    g64 = torch.zeros(it, dtype=torch.float64, device=dev)
+    gb.call("appfis_gb_himeno_f64", ptr64, q64a.data_ptr(), q64b.data_ptr(), nx, ny, nz, nx + 2, it, float(om), g64.data_ptr(),
+            ctypes.byref(ci), sp.cuda_stream)
+    p64 = q64a if ci.value == 0 else q64b
+    del coef64
+
+    def himeno_err(out, g):
+        e = _err(out[..., : nx + 2], p64)
+        e["gosa_rel_err_last"] = float(abs(g[-1].item() - g64[-1].item()) / abs(g64[-1].item()))
+        e["gosa_rel_err_max"] = float(((g - g64).abs() / g64.abs().clamp_min(1e-300)).max().item())
+        return e
+
+    err_p, err_m = himeno_err(out_p, g_p), himeno_err(out_m, g_m)
+    gosa64_last = float(g64[-1].item())
+    del q64a, q64b, p64
     tma_ms = sweep_ms(ptrs, pa, pb, pitch)
     dptrs = (ctypes.c_void_p * 12)(*[coef_d[k].data_ptr() for k in range(12)])
     da, db = p0_d.clone(), p0_d.clone()
@@ -616,13 +695,15 @@ def bench_himeno(torch, gb, W, dev, sp, hbm):
     res["plain"] = {"glups": lups / (ms_p * 1e-3) / 1e9, "ms": ms_p, "bytes_per_lup": 56, "sweep_ms": tma_ms,
                     "kernel": "himeno_tma<plain>", "achieved_gbs": gbs, "frac_of_hbm": gbs / hbm,
                     "traffic": profiled_traffic("himeno_tma<plain>"),
-                    "ring_kernel_sweep_ms_dense_rows": ring_ms, "gosa_last": float(g_p[-1].item())}
+                    "ring_kernel_sweep_ms_dense_rows": ring_ms, "gosa_last": float(g_p[-1].item()),
+                    "gosa_last_fp64": gosa64_last, "error_vs_fp64": err_p}
     b_m = (19 * 30 + 62) / 20.0
     res["mixed_fp16_defect_correction"] = {
         "glups": lups / (ms_m * 1e-3) / 1e9, "ms": ms_m, "bytes_per_lup_avg": b_m, "period": 20,
         "speedup_vs_plain": ms_p / ms_m, "max_abs_diff_vs_plain_fp32": float((out_m - out_p).abs().max().item()),
         "gosa_last": float(g_m[-1].item()),
-        "gosa_rel_diff_vs_plain": float(((g_m - g_p).abs() / g_p.abs().clamp_min(1e-300)).max().item())}
+        "gosa_rel_diff_vs_plain": float(((g_m - g_p).abs() / g_p.abs().clamp_min(1e-300)).max().item()),
+        "error_vs_fp64": err_m}
     res["workload"] = "himeno 257x257x513 FP32, 400 iterations, per-sweep FP64 gosa; rows padded to %d" % pitch
     return res
 
@@ -656,6 +737,15 @@ def bench_fdtd(torch, gb, W, dev, sp, hbm):
                               ctypes.byref(ci), sp.cuda_stream)
         return _time(torch, sp, one, reps=1) / n
 
+    # FP64 reference of the same 200 steps (appfis_gb_star_r4_f64, the weights in double)
+    w64 = (ctypes.c_double * 5)(*W.fdtd_weights())
+    x64 = f32.double()
+    y64 = x64.clone()
+    gb.call("appfis_gb_star_r4_f64", x64.data_ptr(), y64.data_ptr(), nx, ny, nz, nx + 8, it, 1, 0.0, w64, ctypes.byref(ci),
+            sp.cuda_stream)
+    r64 = x64 if ci.value == 0 else y64
+    err32, err16 = _err(o32, r64), _err(o16, r64)
+    del x64, y64, r64
     s32 = steps_only(a, b, 0, 0)
     s16 = steps_only(ha, hb, 3, 0)
     # one step of each tile (APPFIS_GB_STAR_TMA_X4 / TMA_X2 / VEC), averaged over 10
@@ -668,12 +758,12 @@ def bench_fdtd(torch, gb, W, dev, sp, hbm):
     res["workload"] = "fdtd3d radius-4 star 512^3, 200 steps of u <- u + 0.1*L8(u), zero halo of 4"
     res["plain_fp32"] = {"glups": lups / (ms32 * 1e-3) / 1e9, "ms": ms32, "bytes_per_lup": 8, "sweep_ms": s32,
                          "kernel": "star_r4_tma<float>", "achieved_gbs": g32, "frac_of_hbm": g32 / hbm,
-                         "traffic": profiled_traffic("star_r4_tma<float>")}
+                         "traffic": profiled_traffic("star_r4_tma<float>"), "error_vs_fp64": err32}
     res["fp16_storage"] = {"glups": lups / (ms16 * 1e-3) / 1e9, "ms": ms16, "bytes_per_lup": 4, "sweep_ms": s16,
                            "kernel": "star_r4_tma<half>", "achieved_gbs": g16, "frac_of_hbm": g16 / hbm,
                            "traffic": profiled_traffic("star_r4_tma<half>"), "speedup_vs_plain": ms32 / ms16,
                            "step_ms_by_tile": tiles,
-                           "max_abs_diff_vs_fp32": float((o16 - o32).abs().max().item())}
+                           "max_abs_diff_vs_fp32": float((o16 - o32).abs().max().item()), "error_vs_fp64": err16}
     return res
 
 
@@ -738,12 +828,48 @@ def bench_flood(torch, gb, W, dev, sp):
     assert int(status.item()) == 0
     same = bool((st_k == st).all()) and all(torch.equal(final_state(k, st_k[k]), dense[k]) for k in range(nd))
     prm.flags = 0
+    # FP64 reference of the same batch (the FP64 form matches the reference CPU path to 1e-9);
+    # run with the dry strips left out, which leaves every field bit-identical
+    bufs64, descs64 = [], (_lib.FloodDomain * nd)()
+    for k, (dem, h) in enumerate(doms):
+        ny, nx = dem.shape
+        pitch = ((nx + 2 + 15) // 16) * 16
+        f = torch.empty((8, ny + 2, pitch), dtype=torch.float64, device=dev)
+        bufs64.append(f)
+        d = descs64[k]
+        d.nx, d.ny, d.pitch = nx, ny, pitch
+        d.h[0], d.h[1], d.qx[0], d.qx[1], d.qy[0], d.qy[1] = [f[m].data_ptr() for m in range(6)]
+        d.dem, d.n2 = f[6].data_ptr(), f[7].data_ptr()
+        gb.call("appfis_gb_flood_setup", ctypes.byref(d), _lib.F64, inter[k][0].data_ptr(), inter[k][1].data_ptr(), None, None,
+                c["manning"], sp.cuda_stream)
+    prm64 = _lib.FloodParams(c["dx"], c["courant"], c["hextra"], c["t_end"], c["t_end"], c["time_step"], 0.0, 0)
+    prm64.flags = _lib.FLOOD_SKIP_DRY
+    steps64 = torch.zeros(nd, dtype=torch.int32, device=dev)
+    ms64 = _time(torch, sp, lambda: gb.call("appfis_gb_flood_run", descs64, nd, _lib.F64, ctypes.byref(prm64), None,
+                                            steps64.data_ptr(), None, status.data_ptr(), sp.cuda_stream), reps=1, warmup=0)
+    assert int(status.item()) == 0
+    st64 = steps64.cpu().numpy().astype(np.int64)
+    l1_rel, hmax, m64 = [], 0.0, []
+    for k in range(nd):
+        ny, nx = doms[k][0].shape
+        h32 = dense[k][0][1:ny + 1, 1:nx + 1].double()
+        h64 = bufs64[k][int(st64[k]) & 1][1:ny + 1, 1:nx + 1]
+        vol = float(h64.sum().item())
+        m64.append(vol)
+        l1_rel.append(float((h32 - h64).abs().sum().item()) / vol)
+        hmax = max(hmax, float((h32 - h64).abs().max().item()))
+    err_flood = {"l1_depth_err_over_volume_max": max(l1_rel), "l1_depth_err_over_volume_mean": float(np.mean(l1_rel)),
+                 "max_abs_depth_err_m": hmax,
+                 "mass_rel_change_fp64_max": max(abs(a - b) / a for a, b in zip(m0, m64)),
+                 "fp64_steps_min": int(st64.min()), "fp64_steps_max": int(st64.max()), "fp64_ms": ms64,
+                 "note": "FP32 batch vs the FP64 batch at t = 600 s (same domains; both land on t_end exactly)"}
+    del bufs64
     ms_s = _time(torch, sp, one_by_one, reps=1)
     setup_ms = _time(torch, sp, setup, reps=1)
     return {"workload": "flood model, 32 domains (sides 512-3072, %.1f M cells), fractal DEM, to t = 600 s" % (cells.sum() / 1e6),
             "batched_fp32": {"glups": cell_steps / ((ms_b - setup_ms) * 1e-3) / 1e9, "ms": ms_b - setup_ms,
                              "steps_min": int(st.min()), "steps_max": int(st.max()), "cell_steps": cell_steps,
-                             "mass_rel_change_max": drift},
+                             "mass_rel_change_max": drift, "error_vs_fp64": err_flood},
             "batched_fp32_skip_dry": {"glups": cell_steps / ((ms_k - setup_ms) * 1e-3) / 1e9, "ms": ms_k - setup_ms,
                                       "fields_identical_to_full_sweep": same,
                                       "note": "strips whose cells and neighbour strips are exactly dry are left out "

@@ -206,6 +206,25 @@ APPFIS_GB_API int appfis_gb_star_r4(void* a, void* b, int dtype, int nx, int ny,
                                     float coeff, const float* weights, int tile, int zchunk, int* cur_index,
                                     void* stream);
 
+/* ----------------------------------------------------------------------------- FP64 sweeps */
+/* The heat, Himeno and radius-4 star functors instantiated with double, every multiply and add
+ * rounded separately in the reference's order: bit-identical to the reference's CPU path built
+ * with double (its functors are templates on the element type; HeatDiffusion itself runs in
+ * double, HeatDiffusion/src/heat_appfis.hpp:72,166-174).  Same layouts and arguments as the
+ * FP32 entry points above (a, b: the two buffers; pitch in elements; ghost ring held in both).
+ * They are also the precision reference that the FP32, FP16-storage, mixed-precision and
+ * time-blocked forms state their error against.  Bounded by the FP64 pipe (not a fast path). */
+APPFIS_GB_API int appfis_gb_heat2d_f64(double* a, double* b, int nx, int ny, int pitch, int iters, double cx, double cy,
+                                       int* cur_index, void* stream);
+/* Himeno/src/himeno_appfis.hpp:178-198 in double; coef: 12 device pointers as appfis_gb_himeno;
+ * dev_gosa (optional, `iters` doubles): sum of ss^2 per sweep, fixed-order (deterministic). */
+APPFIS_GB_API int appfis_gb_himeno_f64(const double* const* coef, double* p, double* wrk2, int nx, int ny, int nz, int pitch,
+                                       int iters, double omega, double* dev_gosa, int* cur_index, void* stream);
+/* FDTD3d/src/fdtd3d_appfis.hpp:129-143 (mode 0, coefficient `coeff`) or the weighted form
+ * (mode 1, 5 double weights) in double, halo width 4. */
+APPFIS_GB_API int appfis_gb_star_r4_f64(double* a, double* b, int nx, int ny, int nz, int pitch, int iters, int mode,
+                                        double coeff, const double* weights, int* cur_index, void* stream);
+
 /* ----------------------------------------------------------------------------- Triton flood model */
 /* Replaces the reference's Triton time loop (Triton/src/triton_appfis.hpp:316-386: CFL dt functor +
  * Execute2DReduce(MIN) + host clamp, sqrt/RHS reset, X and Y Roe-type flux functors, update +

@@ -2,11 +2,14 @@
 (oracle/_ref: the reference's headers built with APPFIS_CPU and a single-rank MPI stand-in)
 on small seeded inputs.  Needs the reference tree (builds oracle/_ref first).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # the small fixtures (seconds)
+    python tests/golden/make_golden.py --full-gol # the full GameOfLife workload (minutes)
 
 Each fixture holds the inputs, the reference's outputs and its printed scalars; tests check the
 oracle restatement and the GPU kernels against them.
 """
+import hashlib
+import json
 import os
 import sys
 
@@ -68,8 +71,29 @@ def triton(nx, ny, steps, seed):
          steps=np.int64(res["steps"]))
 
 
+def gol_full(nx=16384, ny=16384, gens=2000, seed=42, p=0.3):
+    """The benchmark's GameOfLife workload through the reference's own CPU path, all host
+    threads: the final population and a SHA-256 of the final interior (u8, x fastest) go to a
+    small JSON fixture, so a GPU run of the same 5.4e11 cell updates can be checked bit for bit
+    without the 268 MB state."""
+    cells = W.gol_cells(nx, ny, p, seed)
+    res, (out,) = O.run_ref("gol", [nx, ny, gens, os.cpu_count(), "{in0}", "{out0}"], [cells], [(np.uint8, None)])
+    rec = {"nx": nx, "ny": ny, "gens": gens, "seed": seed, "p": p, "rule": "reference (S234, stale carry)",
+           "live": int(res["live"]), "live_recount": int(out.sum(dtype=np.int64)),
+           "sha256": hashlib.sha256(np.ascontiguousarray(out).tobytes()).hexdigest(),
+           "input_sha256": hashlib.sha256(np.ascontiguousarray(cells).tobytes()).hexdigest(),
+           "reference_seconds": res["seconds"], "threads": os.cpu_count()}
+    name = "gol_%dx%d_g%d.json" % (nx, ny, gens)
+    with open(os.path.join(HERE, name), "w") as f:
+        json.dump(rec, f, indent=1)
+    print(name, rec)
+
+
 if __name__ == "__main__":
     build_ref.build()
+    if "--full-gol" in sys.argv:
+        gol_full()
+        sys.exit(0)
     gol(37, 29, 9, 5)
     gol(64, 48, 17, 6)
     heat2d(19, 23, 17, 3)

@@ -71,9 +71,11 @@ def test_u8_vs_oracle(gb, torch_cuda, nx, ny, gens, rule):
 
 # 16+ generations run the time-blocked kernel: 30-word tile columns (1056 = 33 words: a second
 # column of 3 words; 960 = exactly one column; 32 = one word, fewer rows than the row halo),
-# partial last row tiles, and 2-3 launches plus a remainder.
+# partial last row tiles, 1-7 time-blocked launches (odd counts of 3 or more go round three
+# buffer pairs before ping-ponging) plus a remainder.
 @pytest.mark.parametrize("nx,ny,gens", [(32, 1, 3), (32, 7, 5), (64, 40, 11), (1056, 66, 9), (2048, 130, 8), (96, 257, 21),
-                                        (1056, 300, 33), (960, 70, 16), (32, 20, 16), (2048, 700, 48), (160, 1100, 17)])
+                                        (1056, 300, 33), (960, 70, 16), (32, 20, 16), (2048, 700, 48), (160, 1100, 17),
+                                        (256, 300, 80), (320, 140, 85), (128, 64, 112), (64, 520, 64)])
 @pytest.mark.parametrize("rule", [0, 1])
 def test_bits_vs_oracle(gb, torch_cuda, nx, ny, gens, rule):
     cells = W.gol_cells(nx, ny, 0.3, nx + 3 * ny)

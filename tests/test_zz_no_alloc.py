@@ -6,7 +6,7 @@ loop).
 appfis_gb_reduce_noalloc is called through the C ABI and must give what appfis_gb_reduce gives
 on the same field — MAX and MIN exactly, SUM within the 1e-12 relative tolerance of the other
 reduction tests — on two calls in a row (the second one reuses the fixed scratch left by the
-first); the oracle's value is checked as well.  This file runs last so that a failure here
+first); MAX and MIN are also checked against the oracle, SUM against a double sum of the box.  This file runs last so that a failure here
 cannot hide any other test."""
 import ctypes
 
@@ -47,6 +47,10 @@ def test_noalloc_matches_workspace_reduction(gb, torch_cuda, dtype, code, shape,
                 assert abs(g - w) <= 1e-12 * max(1.0, abs(w)), (op, call, g, w)
             else:
                 assert g == w, (op, call, g, w)
-        o = O.reduce(a if len(shape) == 3 else a[None], list(box) + ([0, 1] if len(box) == 4 else []),
-                     ("max", "min", "sum")[op])
+        a3 = a if len(shape) == 3 else a[None]
+        b6 = list(box) + ([0, 1] if len(box) == 4 else [])
+        if op == 2:  # the engine sums in double (int64 for int), the oracle in the element type like the reference
+            o = float(a3[b6[4]:b6[5], b6[2]:b6[3], b6[0]:b6[1]].astype(np.float64).sum())
+        else:
+            o = O.reduce(a3, b6, ("max", "min", "sum")[op])
         assert abs(got.item() - o) <= 1e-12 * max(1.0, abs(o)), (op, got.item(), o)
