@@ -37,6 +37,10 @@ namespace APPFIS
 		int neighbours[6] = { PROC_NULL, PROC_NULL, PROC_NULL, PROC_NULL, PROC_NULL, PROC_NULL };
 		cudaStream_t stream = 0;
 		bool initialized = false;
+		// set once a Config is routed to a hand-written kernel (Fast.hpp): run the sweeps it
+		// deferred / also free its buffers
+		void (*flushFast)() = nullptr;
+		void (*releaseFast)() = nullptr;
 
 		static Context& Get()
 		{
@@ -96,6 +100,7 @@ namespace APPFIS
 	inline void Finalize()
 	{
 		Context& c = Context::Get();
+		if (c.releaseFast) c.releaseFast();
 		if (c.stream) cudaStreamSynchronize(c.stream);
 	}
 

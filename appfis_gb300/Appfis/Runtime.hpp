@@ -32,6 +32,7 @@
 #include <type_traits>
 
 #include "Config.hpp"
+#include "Fast.hpp"
 #include "Grid.hpp"
 
 namespace APPFIS
@@ -322,6 +323,7 @@ namespace APPFIS
 	template<typename T>
 	void FinalizeExecution(Grid<T>& grid)
 	{
+		detail::FlushFast();
 		ExecutionFlag() = false;
 		grid.DownloadCurrent(GetCudaStream());
 	}
@@ -336,6 +338,14 @@ namespace APPFIS
 	template<typename T, typename... TArgs>
 	void Execute1D(Config<T>& config, TArgs... args)
 	{
+		if (detail::FastState* fs = detail::FastFind(&config))  // routed by UseFastKernel
+		{
+			detail::FlushFast(fs);
+			detail::FastCall(*fs, config, args...);
+			detail::FastAfter(config);
+			return;
+		}
+		detail::FlushFast();  // a functor sweep reads the grids as the deferred sweeps leave them
 		const int x0 = config.GetStartX(), x1 = config.GetEndX();
 		if (x1 > x0)
 			detail::Functor1D<typename detail::KArg<TArgs>::type...><<<detail::Blocks(x1 - x0, 256), 256, 0, GetCudaStream()>>>(
@@ -346,6 +356,14 @@ namespace APPFIS
 	template<typename T, typename... TArgs>
 	void Execute2D(Config<T>& config, TArgs... args)
 	{
+		if (detail::FastState* fs = detail::FastFind(&config))  // routed by UseFastKernel
+		{
+			detail::FlushFast(fs);
+			detail::FastCall(*fs, config, args...);
+			detail::FastAfter(config);
+			return;
+		}
+		detail::FlushFast();  // a functor sweep reads the grids as the deferred sweeps leave them
 		const int x0 = config.GetStartX(), x1 = config.GetEndX(), y0 = config.GetStartY(), y1 = config.GetEndY();
 		if (x1 > x0 && y1 > y0)
 		{
@@ -371,6 +389,14 @@ namespace APPFIS
 	template<typename T, typename... TArgs>
 	void Execute3D(Config<T>& config, TArgs... args)
 	{
+		if (detail::FastState* fs = detail::FastFind(&config))  // routed by UseFastKernel
+		{
+			detail::FlushFast(fs);
+			detail::FastCall(*fs, config, args...);
+			detail::FastAfter(config);
+			return;
+		}
+		detail::FlushFast();  // a functor sweep reads the grids as the deferred sweeps leave them
 		const int x0 = config.GetStartX(), x1 = config.GetEndX(), y0 = config.GetStartY(), y1 = config.GetEndY();
 		const int z0 = config.GetStartZ(), z1 = config.GetEndZ();
 		if (x1 > x0 && y1 > y0 && z1 > z0)
@@ -432,6 +458,7 @@ namespace APPFIS
 				std::cerr << "APPFIS engine: Execute*DReduce needs InitializeExecution(grid) first." << std::endl;
 				std::exit(EXIT_FAILURE);
 			}
+			FlushFast();
 			Array<T>* a = grid.GetSubGridCPU();
 			const int box[6] = { config.GetStartX(), config.GetEndX(),
 				nDim > 1 ? config.GetStartY() : 0, nDim > 1 ? config.GetEndY() : 1,
@@ -472,6 +499,7 @@ namespace APPFIS
 	template<typename T>
 	void HaloExchange(Grid<T>* grid)
 	{
+		detail::FlushFast();
 		detail::RefreshGhosts(grid, true);
 		grid->Swap();
 	}

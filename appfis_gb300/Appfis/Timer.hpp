@@ -30,10 +30,15 @@ namespace APPFIS
 	public:
 		Timer() {}
 
-		void Start(std::string category) { _start[Key(category)] = Clock::now(); }
+		void Start(std::string category)
+		{
+			if (Context::Get().flushFast) Context::Get().flushFast();  // deferred sweeps belong before the bracket
+			_start[Key(category)] = Clock::now();
+		}
 
 		void Stop(std::string category)
 		{
+			if (Context::Get().flushFast) Context::Get().flushFast();  // run the sweeps a fast kernel deferred
 			if (Context::Get().stream) cudaStreamSynchronize(Context::Get().stream);
 			const std::string k = Key(category);
 			std::map<std::string, Clock::time_point>::iterator it = _start.find(k);

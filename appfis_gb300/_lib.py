@@ -36,6 +36,8 @@ SIGNATURES = {
     "appfis_gb_life_pack": [_P, _P, _i, _i, _P],
     "appfis_gb_life_unpack": [_P, _P, _i, _i, _P],
     "appfis_gb_life_bits": [_P, _P, _i, _i, _i, _i, _P, _P],
+    "appfis_gb_life_from_i32": [_P, _i, _i, _P, _i, _i, _P],
+    "appfis_gb_life_to_i32": [_P, _i, _i, _P, _i, _i, _P],
     "appfis_gb_life_population_u8": [_P, _i64, _P, _P],
     "appfis_gb_life_population_bits": [_P, _i64, _P, _P],
     "appfis_gb_life_job": [_P, _P, _i, _i, _i, _i, _i, _P],

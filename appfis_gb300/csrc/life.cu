@@ -407,6 +407,30 @@ __global__ void life_unpack(const uint32_t* __restrict__ bits, uint8_t* __restri
     p[1] = make_uint4(v[4], v[5], v[6], v[7]);
 }
 
+// The reference's layout: int cells 0/1 on a (nx + 2g) x (ny + 2g) grid with a periodic ghost
+// ring of width g (GameOfLife/src/game_appfis.hpp:58-62).  From it: the u8 interior; into it:
+// every padded cell from the interior cell it wraps to (the ghost ring as the periodic exchange
+// leaves it, corners included).
+__global__ void life_from_i32(const int32_t* __restrict__ f, int px, int g, uint8_t* __restrict__ cells, int nx, int ny)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nx) return;
+    for (int j = blockIdx.y; j < ny; j += gridDim.y) cells[(size_t)j * nx + i] = __ldg(f + (size_t)(j + g) * px + i + g) != 0;
+}
+
+__global__ void life_to_i32(const uint8_t* __restrict__ cells, int nx, int ny, int32_t* __restrict__ f, int px, int g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nx + 2 * g) return;
+    int si = (i - g) % nx;
+    if (si < 0) si += nx;
+    for (int j = blockIdx.y; j < ny + 2 * g; j += gridDim.y) {
+        int sj = (j - g) % ny;
+        if (sj < 0) sj += ny;
+        f[(size_t)j * px + i] = __ldg(cells + (size_t)sj * nx + si);
+    }
+}
+
 // Population: popcount over 32-bit words (u8 cells are 0/1, so popc of 4 bytes = live bytes).
 __global__ void popcount_words(const uint32_t* __restrict__ words, size_t n, unsigned long long* __restrict__ out)
 {
@@ -596,6 +620,24 @@ int appfis_gb_life_unpack(const uint32_t* bits, uint8_t* cells, int nx, int ny, 
     size_t nw = (size_t)nx * ny / 32;
     life_unpack<<<gb::ceil_div(nw, 256), 256, 0, gb::as_stream(stream)>>>(bits, cells, nw);
     return gb::launched("life_unpack");
+}
+
+int appfis_gb_life_from_i32(const int32_t* padded, int px, int ghost, uint8_t* cells, int nx, int ny, void* stream)
+{
+    if (!padded || !cells || nx < 1 || ny < 1 || ghost < 0 || ghost > nx || ghost > ny || px < nx + 2 * ghost)
+        return gb::fail(APPFIS_GB_EINVAL, "life_from_i32: bad arguments");
+    dim3 grd(gb::ceil_div(nx, 256), std::min(ny, 65535));
+    life_from_i32<<<grd, 256, 0, gb::as_stream(stream)>>>(padded, px, ghost, cells, nx, ny);
+    return gb::launched("life_from_i32");
+}
+
+int appfis_gb_life_to_i32(const uint8_t* cells, int nx, int ny, int32_t* padded, int px, int ghost, void* stream)
+{
+    if (!padded || !cells || nx < 1 || ny < 1 || ghost < 0 || ghost > nx || ghost > ny || px < nx + 2 * ghost)
+        return gb::fail(APPFIS_GB_EINVAL, "life_to_i32: bad arguments");
+    dim3 grd(gb::ceil_div(nx + 2 * ghost, 256), std::min(ny + 2 * ghost, 65535));
+    life_to_i32<<<grd, 256, 0, gb::as_stream(stream)>>>(cells, nx, ny, padded, px, ghost);
+    return gb::launched("life_to_i32");
 }
 
 int appfis_gb_life_population_u8(const uint8_t* cells, int64_t n, int64_t* dev_count, void* stream)

@@ -268,7 +268,8 @@ def apps_unchanged():
     """The reference's sample applications, unchanged, on three builds on this machine: the
     reference's CPU path (OpenMP, every core), the reference's own GPU path (APPFIS_CUDA for
     sm_103a) and the drop-in headers (generic functor kernels of this engine; both GPU builds
-    with nvcc's default FMA contraction).  GLUP/s from each
+    with nvcc's default FMA contraction); GameOfLife, Himeno and FDTD3d also with their one
+    UseFastKernel line (the hand-written kernels; appfis_gb300/Appfis/Fast.hpp).  GLUP/s from each
     application's own COMPUTE timer (its printed `Compute:` seconds; the flood application: its `BLUPS:`
     line, since its step count follows the time step)."""
     import re
@@ -289,6 +290,7 @@ def apps_unchanged():
         ref = dict(zip(apps, ex.map(build_ref.app_ref_exe, apps)))
         refgpu = dict(zip(apps, ex.map(build_ref.app_refgpu_exe, apps)))
     gbx = build_apps.build(apps, exact=False)  # nvcc's default contraction, like the reference's GPU build
+    fast = build_apps.build(build_apps.FAST_APPS, fast=True)  # the same sources plus their UseFastKernel line
     cores = os.cpu_count() or 1
     out = {}
     from appfis_gb300 import workloads as W
@@ -296,8 +298,11 @@ def apps_unchanged():
         W.write_triton_case(td, 1024, 1024, 11, 600)
         for app, args, lups in cases:
             row = {"args": " ".join(args) if lups else "1024x1024 synthetic case (fractal DEM, point source), 600 s"}
-            for name, exe, extra in (("reference_cpu", ref[app], ["-thread=%d" % cores]), ("reference_gpu", refgpu[app], []),
-                                     ("dropin_gpu", gbx[app], [])):
+            builds = [("reference_cpu", ref[app], ["-thread=%d" % cores]), ("reference_gpu", refgpu[app], []),
+                      ("dropin_gpu", gbx[app], [])]
+            if app in fast:
+                builds.append(("dropin_fast_kernel_gpu", fast[app], []))
+            for name, exe, extra in builds:
                 r = subprocess.run([exe] + args + extra, capture_output=True, text=True, timeout=900, cwd=td)
                 m = re.search(r"^Compute:\s*(\S+)", r.stdout, re.M)
                 b = re.search(r"^BLUPS:\s*(\S+)", r.stdout, re.M)
@@ -816,9 +821,10 @@ def bench_flood(torch, gb, W, dev, sp):
         ny, nx = doms[k][0].shape
         m1.append(float(bufs[k][b][1:ny + 1, 1:nx + 1].double().sum().item()))
     drift = max(abs(a - b) / a for a, b in zip(m0, m1))
-    def final_state(k, n):  # h, qx, qy of domain k after n steps (buffers h0 h1 qx0 qx1 qy0 qy1 dem n2)
+    def final_state(k, n):  # interiors of h, qx, qy of domain k after n steps (buffers h0 h1 qx0 qx1 qy0 qy1 dem n2)
         b = int(n) & 1
-        return torch.stack([bufs[k][b], bufs[k][2 + b], bufs[k][4 + b]])
+        ny, nx = doms[k][0].shape
+        return torch.stack([bufs[k][b], bufs[k][2 + b], bufs[k][4 + b]])[:, 1:ny + 1, 1:nx + 1]
 
     dense = [final_state(k, st[k]).clone() for k in range(nd)]
     # the same batch leaving out strips that are dry with dry neighbours (bit-identical fields)
@@ -852,7 +858,7 @@ def bench_flood(torch, gb, W, dev, sp):
     l1_rel, hmax, m64 = [], 0.0, []
     for k in range(nd):
         ny, nx = doms[k][0].shape
-        h32 = dense[k][0][1:ny + 1, 1:nx + 1].double()
+        h32 = dense[k][0].double()
         h64 = bufs64[k][int(st64[k]) & 1][1:ny + 1, 1:nx + 1]
         vol = float(h64.sum().item())
         m64.append(vol)

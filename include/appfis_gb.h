@@ -129,6 +129,16 @@ APPFIS_GB_API int appfis_gb_life_u8(uint8_t* a, uint8_t* b, int nx, int ny, int 
 APPFIS_GB_API int appfis_gb_life_pack(const uint8_t* cells, uint32_t* bits, int nx, int ny, void* stream);
 APPFIS_GB_API int appfis_gb_life_unpack(const uint32_t* bits, uint8_t* cells, int nx, int ny, void* stream);
 APPFIS_GB_API int appfis_gb_life_bits(uint32_t* a, uint32_t* b, int nx, int ny, int gens, int rule, int* cur_index, void* stream);
+/* The reference's own layout (GameOfLife/src/game_appfis.hpp:58-62: int cells on a grid padded by
+ * a periodic ghost ring of width `ghost`, row pitch px >= nx + 2*ghost, (ny + 2*ghost) rows) to the
+ * u8 interior above, and back: to_i32 writes every padded cell from the interior cell it wraps to,
+ * i.e. the interior plus the ghost ring as the reference's periodic exchange leaves it
+ * (Appfis/Communication.hpp:612-678).  The drop-in's GameOfLife fast path uses these at the edges
+ * of a run of generations. */
+APPFIS_GB_API int appfis_gb_life_from_i32(const int32_t* padded, int px, int ghost, uint8_t* cells, int nx, int ny,
+                                          void* stream);
+APPFIS_GB_API int appfis_gb_life_to_i32(const uint8_t* cells, int nx, int ny, int32_t* padded, int px, int ghost,
+                                        void* stream);
 /* Population (Execute2DReduce SUM of the cells, game_appfis.hpp:84) into an int64 device location. */
 APPFIS_GB_API int appfis_gb_life_population_u8(const uint8_t* cells, int64_t n, int64_t* dev_count, void* stream);
 APPFIS_GB_API int appfis_gb_life_population_bits(const uint32_t* bits, int64_t nwords, int64_t* dev_count, void* stream);

@@ -30,12 +30,38 @@ def _newest_input(src):
     return max(os.path.getmtime(f) for f in files)
 
 
-def build_one(app, exact=True):
+# The one line an application adds to route its Execute*D loop to a hand-written kernel
+# (appfis_gb300/Appfis/Fast.hpp), inserted right after its `config.GridsToUpdate(...);`.
+FAST_LINE = {"GameOfLife": "APPFIS::UseFastKernel(config, APPFIS::FAST_LIFE);",
+             "Himeno": "APPFIS::UseFastKernel(config, APPFIS::FAST_HIMENO);",
+             "FDTD3d": "APPFIS::UseFastKernel(config, APPFIS::FAST_STAR_R4);"}
+FAST_APPS = sorted(FAST_LINE)
+
+
+def fast_source(app):
+    """<app>.fast.cpp: the flattened application with its one opt-in line added."""
+    src = source(app)
+    dst = os.path.join(APPS_DIR, "%s.fast.cpp" % app)
+    text = open(src).read()
+    lines = text.split("\n")
+    hits = [n for n, l in enumerate(lines) if l.strip().startswith("config.GridsToUpdate(")]
+    if len(hits) != 1:
+        raise RuntimeError("%s: expected one config.GridsToUpdate line, found %d" % (app, len(hits)))
+    indent = lines[hits[0]][: len(lines[hits[0]]) - len(lines[hits[0]].lstrip())]
+    lines.insert(hits[0] + 1, indent + FAST_LINE[app])
+    out = "\n".join(lines)
+    if not (os.path.exists(dst) and open(dst).read() == out):
+        with open(dst, "w") as f:
+            f.write(out)
+    return dst
+
+
+def build_one(app, exact=True, fast=False):
     """exact: -fmad=false (the functors' multiplies and adds rounded separately, as on the
     reference's CPU build); otherwise nvcc's default contraction, as the reference's own GPU
-    build uses (for timing against it)."""
-    src = source(app)
-    exe = os.path.join(APPS_DIR, "%s.%s" % (app, "gb" if exact else "gbfma"))
+    build uses (for timing against it).  fast: the application with its UseFastKernel line."""
+    src = fast_source(app) if fast else source(app)
+    exe = os.path.join(APPS_DIR, "%s.%s" % (app, "fast" if fast else ("gb" if exact else "gbfma")))
     stamp = exe + ".arch"
     if (os.path.exists(exe) and os.path.exists(stamp) and open(stamp).read() == platform.machine()
             and os.path.getmtime(exe) >= _newest_input(src)):
@@ -55,6 +81,6 @@ def available():
     return all(os.path.exists(source(a)) for a in APPS)
 
 
-def build(apps=APPS, exact=True):
+def build(apps=APPS, exact=True, fast=False):
     with ThreadPoolExecutor(max_workers=len(apps)) as ex:
-        return dict(zip(apps, ex.map(lambda a: build_one(a, exact), apps)))
+        return dict(zip(apps, ex.map(lambda a: build_one(a, exact, fast), apps)))

@@ -8,6 +8,14 @@ the Triton flood application, run on a synthetic case through its own readers (k
 configuration, ASCII DEM with its 6-line header, initial depth file, point source with a
 hydrograph), must write the same h/u/v fields (6 decimals, the applications' output format).
 
+The same applications with ONE added line, APPFIS::UseFastKernel(config, ...) after their
+GridsToUpdate (appfis_gb300/Appfis/Fast.hpp), run their Execute*D loops on the hand-written
+kernels (GameOfLife: the bit-packed time-blocked or the u8 sweep; Himeno: the TMA-staged sweep,
+on 128-byte-pitched copies where the application's rows are not 16-byte aligned; FDTD3d: the
+TMA-staged radius-4 star) and must print what the unchanged build prints: GameOfLife Live Count
+and Himeno Sum identical to the unchanged build (and to the reference as above); FDTD3d's
+written field identical to the reference CPU build's.
+
 Needs oracle/_ref/apps/ (flattened from the reference tree by oracle/build_ref.py)."""
 import os
 import re
@@ -93,3 +101,45 @@ def test_triton_application_case_files(exes, tmp_path, nx, ny, seed, duration):
         assert a.shape == (ny, nx)
         # 6 printed decimals; cbrt/sqrt may differ in the last bit between the CUDA and host libraries
         assert np.abs(a - b).max() <= 2e-6
+
+
+@pytest.fixture(scope="module")
+def fast_exes(gb):
+    return build_apps.build(build_apps.FAST_APPS, fast=True)
+
+
+@pytest.mark.parametrize("app,args,keys,rtol", [
+    ("GameOfLife", ["-dimx=320", "-dimy=200", "-iteration=50"], ["Live Count"], 0),   # bit-packed: 3 x 16 + 2 generations
+    ("GameOfLife", ["-dimx=67", "-dimy=45", "-iteration=31"], ["Live Count"], 0),     # u8 cells (67 is not a multiple of 32)
+    ("GameOfLife", ["-dimx=64", "-dimy=64", "-iteration=7"], ["Live Count"], 0),      # fewer generations than one time block
+    ("Himeno", ["-dimx=126", "-dimy=65", "-dimz=100", "-iteration=20"], ["Sum"], 2e-4),  # 128-float rows: on the grids
+    ("Himeno", ["-dimx=65", "-dimy=65", "-dimz=129", "-iteration=20"], ["Sum"], 2e-4),   # 67-float rows: padded copies
+])
+def test_fast_kernel_application_outputs_match(exes, fast_exes, tmp_path, app, args, keys, rtol):
+    gbx, ref = exes
+    f = values(run(fast_exes[app], args + ["-output"], str(tmp_path)), keys)
+    u = values(run(gbx[app], args + ["-output"], str(tmp_path)), keys)
+    b = values(run(ref[app], args + ["-output", "-thread=4"], str(tmp_path)), keys)
+    assert f == u  # same fields as the functor path, same engine reduction
+    for k in keys:
+        if rtol == 0:
+            assert f[k] == b[k]
+        else:
+            assert float(f[k]) == pytest.approx(float(b[k]), rel=rtol), (k, f[k], b[k])
+
+
+@pytest.mark.parametrize("dims", [(64, 48, 40), (61, 37, 23)])
+def test_fast_kernel_fdtd_field_matches_reference(exes, fast_exes, tmp_path, dims):
+    """FDTD3d with its fast-kernel line writes the same field (6 decimals of every value after
+    10 steps) as the reference's CPU build: the radius-4 star in the reference form is
+    bit-identical (64-wide rows: TMA-staged tile; 61-wide rows: the unaligned fallback tiles)."""
+    gbx, ref = exes
+    args = ["-dimx=%d" % dims[0], "-dimy=%d" % dims[1], "-dimz=%d" % dims[2], "-iteration=10", "-output"]
+    texts = {}
+    for name, exe, extra in (("fast", fast_exes["FDTD3d"], []), ("ref", ref["FDTD3d"], ["-thread=4"])):
+        d = tmp_path / name
+        d.mkdir()
+        run(exe, args + extra, str(d))
+        texts[name] = (d / "output" / "output.txt").read_text()
+    assert len(texts["ref"]) > 1000
+    assert texts["fast"] == texts["ref"]
