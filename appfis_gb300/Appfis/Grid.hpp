@@ -12,6 +12,8 @@
 #define APPFIS_GB_GRID_HPP
 
 #include <algorithm>
+#include <fstream>
+#include <string>
 #include <vector>
 
 #include "Array.hpp"
@@ -194,6 +196,44 @@ namespace APPFIS
 		}
 
 		bool IsDeviceView(const Array<T>* a) const { return _dev[0] && (a == &_view[0] || a == &_view[1]); }
+
+		// ---- checkpoint of the device state (no counterpart in the reference, whose applications
+		// save host arrays after Gather: Array::Save/LoadBinaryFile, Appfis/Array.hpp:421-527).
+		// The file holds the padded sub-grid of the current buffer and, for a DUAL grid, the next
+		// buffer after it (raw T values, x fastest): both, because a functor may read the next
+		// buffer's old values (GameOfLife's stale carry).  Callers run any deferred sweeps first
+		// (the engine's SaveDeviceState / LoadDeviceState in Runtime.hpp do).
+		bool SaveDevice(const std::string& path, cudaStream_t st)
+		{
+			if (!_dev[0]) return false;
+			const size_t n = (size_t)_host[0].GetSize();
+			std::vector<T> buf(n * BufferCount());
+			CheckCuda(cudaMemcpyAsync(buf.data(), _dev[_cur], sizeof(T) * n, cudaMemcpyDeviceToHost, st), "checkpoint download");
+			if (BufferCount() == 2)
+				CheckCuda(cudaMemcpyAsync(buf.data() + n, _dev[_next], sizeof(T) * n, cudaMemcpyDeviceToHost, st), "checkpoint download");
+			CheckCuda(cudaStreamSynchronize(st), "checkpoint download");
+			CreateDir(GetParentDir(path.c_str()));
+			std::ofstream out(path.c_str(), std::ios::binary);
+			if (!out.is_open()) return false;
+			out.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)(sizeof(T) * buf.size()));
+			return (bool)out;
+		}
+
+		bool LoadDevice(const std::string& path, cudaStream_t st)
+		{
+			if (!_dev[0]) return false;
+			const size_t n = (size_t)_host[0].GetSize();
+			std::vector<T> buf(n * BufferCount());
+			std::ifstream in(path.c_str(), std::ios::binary);
+			if (!in.is_open()) return false;
+			in.read(reinterpret_cast<char*>(buf.data()), (std::streamsize)(sizeof(T) * buf.size()));
+			if (!in) return false;
+			CheckCuda(cudaMemcpyAsync(_dev[_cur], buf.data(), sizeof(T) * n, cudaMemcpyHostToDevice, st), "checkpoint upload");
+			if (BufferCount() == 2)
+				CheckCuda(cudaMemcpyAsync(_dev[_next], buf.data() + n, sizeof(T) * n, cudaMemcpyHostToDevice, st), "checkpoint upload");
+			CheckCuda(cudaStreamSynchronize(st), "checkpoint upload");
+			return true;
+		}
 
 	private:
 		void FreeDevice()

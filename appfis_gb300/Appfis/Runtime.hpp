@@ -495,6 +495,34 @@ namespace APPFIS
 	template<typename T>
 	void Execute3DReduce(Config<T>& config, T& var, REDUCTION rType, Grid<T>& grid) { detail::Reduce(config, var, rType, grid, 3); }
 
+	// Checkpoint / restart of a grid's device buffers during execution (an engine extension: the
+	// reference's applications checkpoint through host files after Gather, e.g. the Triton
+	// restart inputs h_infile / qx_infile / qy_infile, Triton/src/config_utils.hpp:369-379).
+	// Runs every deferred fast-kernel sweep first; exits with a message when the file cannot be
+	// written or read (or is shorter than the grid's buffers).
+	template<typename T>
+	void SaveDeviceState(Grid<T>& grid, const std::string& path)
+	{
+		detail::FlushFast();
+		if (!grid.SaveDevice(path, GetCudaStream()))
+		{
+			std::cerr << "APPFIS engine: cannot write the device state of a grid to " << path
+				<< " (call between InitializeExecution and FinalizeExecution)" << std::endl;
+			std::exit(EXIT_FAILURE);
+		}
+	}
+
+	template<typename T>
+	void LoadDeviceState(Grid<T>& grid, const std::string& path)
+	{
+		detail::FlushFast();
+		if (!grid.LoadDevice(path, GetCudaStream()))
+		{
+			std::cerr << "APPFIS engine: cannot read the device state of a grid from " << path << std::endl;
+			std::exit(EXIT_FAILURE);
+		}
+	}
+
 	// Refresh the ghosts of the grid's next buffer and swap it in (Runtime.hpp:173-189).
 	template<typename T>
 	void HaloExchange(Grid<T>* grid)

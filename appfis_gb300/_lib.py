@@ -16,6 +16,7 @@ F32, F64, I32, F16 = 0, 1, 2, 3
 MAX, MIN, SUM = 0, 1, 2
 LIFE_REFERENCE, LIFE_B3S23 = 0, 1
 FORM_U8, FORM_BITS = 0, 1
+STAR_AUTO, STAR_SCALAR2, STAR_SCALAR4, STAR_TMA_X4, STAR_TMA_X2, STAR_VEC = 0, 2, 4, 8, 9, 10
 
 _P = ctypes.c_void_p
 _i = ctypes.c_int
@@ -28,6 +29,7 @@ SIGNATURES = {
     "appfis_gb_last_error": [],
     "appfis_gb_version": [],
     "appfis_gb_stream_sync": [_P],
+    "appfis_gb_test_stall_next": [_i, ctypes.c_ulonglong],
     "appfis_gb_reduce": [_P, _i, _i, _i, _P, _i, _P, _P],
     "appfis_gb_reduce_host": [_P, _i, _i, _i, _P, _i, _P, _P],
     "appfis_gb_reduce_noalloc": [_P, _i, _i, _i, _P, _i, _P, _P],
@@ -53,6 +55,7 @@ SIGNATURES = {
     "appfis_gb_star_r4_f64": [_P, _P, _i, _i, _i, _i, _i, _i, _d, _P, _P, _P],
     "appfis_gb_flood_run": [_P, _i, _i, _P, _P, _P, _P, _P, _P],
     "appfis_gb_flood_setup": [_P, _i, _P, _P, _P, _P, _d, _P],
+    "appfis_gb_flood_run_sources": [_P, _P, _i, _i, _P, _P, _P, _P, _P, _P],
     "appfis_gb_flood_job": [_i, _P, _P, _P, _P, _P, _P, _d, _P, _i, _P, _P, _P],
 }
 
@@ -61,6 +64,11 @@ class FloodDomain(ctypes.Structure):
     """appfis_gb_flood_domain"""
     _fields_ = [("nx", _i), ("ny", _i), ("pitch", _i), ("h", _P * 2), ("qx", _P * 2), ("qy", _P * 2),
                 ("dem", _P), ("n2", _P)]
+
+
+class FloodSources(ctypes.Structure):
+    """appfis_gb_flood_sources"""
+    _fields_ = [("n", _i), ("nt", _i), ("cells", _P), ("times", _P), ("flows", _P)]
 
 
 class FloodParams(ctypes.Structure):

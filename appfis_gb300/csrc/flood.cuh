@@ -28,7 +28,16 @@ struct Dom {
     long long strip0;  // first global strip of this domain
 };
 
+// Point sources of one domain (device copies of the caller's tables).
+struct SrcDev {
+    int n, nt;            // sources, hydrograph rows
+    const int* cells;     // n cells: the reference's padded sub-grid index row * (nx + 2) + col
+    const double* times;  // nt times (s)
+    const double* flows;  // nt * n flows (m^3/s), row t = the n sources at times[t]
+};
+
 struct Ctl {
+    int src_lo[MAXD];     // hydrograph row of each domain's sources (kept across steps)
     unsigned long long dtbits[2][MAXD];
     double simtime[2][MAXD];
     int pid[2][MAXD];
@@ -47,26 +56,32 @@ struct Params {
     long long total_strips;
     double* dtlog;  // [ndom][max_steps] or null
     unsigned char* zc;  // [2][total_strips] dry-step counters (null: every strip every step)
+    unsigned long long spin_limit;  // polls before a grid-barrier wait gives up
+    int stall_cta;                  // testing: this CTA skips its arrival at the first barrier (-1: none)
+    const SrcDev* srcs;             // [ndom] point sources, or null (no source phase)
 };
 
 constexpr unsigned long long SPIN_LIMIT = 1ull << 25;
 constexpr int STEP_CAP = 1000000;  // steps per domain when the caller sets no limit
 
-__device__ __forceinline__ bool grid_barrier(Ctl* ctl)
+// Grid-wide barrier of the cooperative launch.  Every wait is bounded (`limit` polls, each with
+// a short sleep); a wait that gives up records error 1 and every CTA leaves its loop.  `skip`
+// (testing only) makes this CTA wait without arriving, so that the barrier cannot complete.
+__device__ __forceinline__ bool grid_barrier(Ctl* ctl, unsigned long long limit, bool skip = false)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned* vgen = &ctl->bar_gen;
         const unsigned g = *vgen;
         __threadfence();
-        if (atomicAdd(&ctl->bar_count, 1u) == gridDim.x - 1) {
+        if (!skip && atomicAdd(&ctl->bar_count, 1u) == gridDim.x - 1) {
             ctl->bar_count = 0;
             __threadfence();
             atomicAdd(&ctl->bar_gen, 1u);
         } else {
             unsigned long long n = 0;
             while (*vgen == g) {
-                if (++n > SPIN_LIMIT) {
+                if (++n > limit) {
                     atomicExch(&ctl->error, 1);
                     break;
                 }
@@ -337,6 +352,46 @@ __device__ __forceinline__ void for_strips(unsigned* ctr, long long first, long 
     }
 }
 
+// Point sources of domain d after step n's update (Triton/src/triton_appfis.hpp:352-373 picks
+// the hydrograph rows around the step's start time on the host; :1115-1141 adds
+// flow * dt / dx^2 to h at each source cell), in the reference's operation order, one thread
+// per domain so that sources sharing a cell add in order.  A source cell's strip is marked wet
+// for the dry-strip bookkeeping.
+template <class T>
+__device__ void apply_sources(const Dom<T>& D, const SrcDev& S, Ctl* ctl, int cur, int d, const Params& p, double big)
+{
+    if (S.n <= 0 || !is_active(ctl, cur, d, p)) return;
+    const double dt = step_dt(ctl, cur, d, p, big);
+    if (!(dt > 1e-9 * p.time_step)) return;
+    const double simtime = ctl->simtime[cur][d];
+    int lo = ctl->src_lo[d], hi = S.nt - 1;
+    bool found = false;
+    for (int r = lo; r < hi; r++)
+        if (S.times[r + 1] > simtime) {
+            lo = r;
+            hi = r + 1;
+            found = true;
+            break;
+        }
+    if (!found) lo = hi;
+    ctl->src_lo[d] = lo;
+    T* h = D.h[(ctl->steps[cur][d] + 1) & 1];  // the state step n wrote
+    unsigned char* zwet = p.zc ? p.zc + (size_t)(1 - cur) * p.total_strips : nullptr;
+    for (int s = 0; s < S.n; s++) {
+        const double fl = S.flows[(size_t)lo * S.n + s];
+        double flow = fl;
+        if (lo != hi) {
+            const double fh = S.flows[(size_t)hi * S.n + s];
+            flow = fl + (((fh - fl) * (simtime - S.times[lo])) / (S.times[hi] - S.times[lo]));
+        }
+        const double hs = (flow * dt) / (p.dx * p.dx);
+        const int j = S.cells[s] / (D.nx + 2), i = S.cells[s] - j * (D.nx + 2);
+        T* c = h + (size_t)j * D.px + i;
+        *c = (T)((double)*c + hs);
+        if (zwet) zwet[D.strip0 + (long long)((j - 1) / ROWS) * D.strips_x + (i - 1) / SCOLS] = 0;
+    }
+}
+
 // CTAs per SM the FP32 kernel's register allocation targets (FP64: 1).
 #ifndef FLOOD_F32_MIN_BLOCKS
 #define FLOOD_F32_MIN_BLOCKS 3
@@ -373,7 +428,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
             if (SKIP && p.zc[(size_t)cur * p.total_strips + s] >= 1) return;  // dry input: no fix, no dt
             if (f & 6) phase_a<T>(doms[d], ctl, cur, d, s - doms[d].strip0, f & 1, (f & 2) != 0, (f & 4) != 0, p);
         });
-        if (!grid_barrier(ctl)) return;
+        if (!grid_barrier(ctl, p.spin_limit, n == 0 && (int)blockIdx.x == p.stall_cta)) return;
         if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ticket[cur] = 0;  // next used two steps later, past a barrier
         int active = 0;
         if (threadIdx.x < p.ndom) {
@@ -432,8 +487,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
                 ctl->dtbits[1 - cur][d] = (unsigned long long)__double_as_longlong(big);
             }
         }
-        if (!grid_barrier(ctl)) return;
+        if (!grid_barrier(ctl, p.spin_limit)) return;
         if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ticketb[cur] = 0;  // next used two steps later, past a barrier
+        if (p.srcs) {  // the point sources of step n, seen by the next step's wet/dry fix and dt
+            if (blockIdx.x == 0 && threadIdx.x < p.ndom)
+                apply_sources<T>(doms[threadIdx.x], p.srcs[threadIdx.x], ctl, cur, threadIdx.x, p, big);
+            if (!grid_barrier(ctl, p.spin_limit)) return;
+        }
     }
 }
 
@@ -448,6 +508,7 @@ static __global__ void flood_init_ctl(Ctl* ctl, int ndom, double big, double t0)
         ctl->ticketb[0] = ctl->ticketb[1] = 0;
     }
     if (d < ndom) {
+        ctl->src_lo[d] = 0;
         for (int k = 0; k < 2; k++) {
             ctl->dtbits[k][d] = (unsigned long long)__double_as_longlong(big);
             ctl->simtime[k][d] = t0;

@@ -7,9 +7,9 @@
 namespace flood {
 
 int run_f64(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_params* prm, double* dtlog, int* steps,
-            double* simtime, int* status, cudaStream_t st)
+            double* simtime, int* status, cudaStream_t st, const appfis_gb_flood_sources* srcs)
 {
-    return run<double>(doms, ndom, prm, dtlog, steps, simtime, status, st);
+    return run<double>(doms, ndom, prm, dtlog, steps, simtime, status, st, srcs);
 }
 
 int setup_f64(const appfis_gb_flood_domain* dom, const double* dem, const double* h, const double* qx, const double* qy,

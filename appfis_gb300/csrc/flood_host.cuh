@@ -102,10 +102,69 @@ int setup(const appfis_gb_flood_domain* dom, const double* dem, const double* h,
     return gb::launched("flood_setup");
 }
 
+// Copies the point-source tables of the batch (host arrays) into one device buffer; *out =
+// nullptr when no domain has a source.
+inline int upload_sources(const appfis_gb_flood_domain* doms, const appfis_gb_flood_sources* srcs, int ndom,
+                          const SrcDev** out, cudaStream_t st)
+{
+    *out = nullptr;
+    if (!srcs) return APPFIS_GB_OK;
+    size_t cells = 0, rows = 0, vals = 0;
+    for (int d = 0; d < ndom; d++) {
+        const appfis_gb_flood_sources& S = srcs[d];
+        if (S.n < 0 || (S.n > 0 && (S.nt < 1 || !S.cells || !S.times || !S.flows)))
+            return gb::fail(APPFIS_GB_EINVAL, "flood: domain %d has a bad source table", d);
+        const int px = doms[d].nx + 2;
+        for (int k = 0; k < S.n; k++) {
+            const int j = S.cells[k] / px, i = S.cells[k] - j * px;
+            if (S.cells[k] < 0 || i < 1 || i > doms[d].nx || j < 1 || j > doms[d].ny)
+                return gb::fail(APPFIS_GB_EINVAL, "flood: domain %d source %d is not an interior cell", d, k);
+        }
+        for (int r = 0; r + 1 < S.nt && S.n > 0; r++)
+            if (!(S.times[r + 1] > S.times[r])) return gb::fail(APPFIS_GB_EINVAL, "flood: domain %d hydrograph times must increase", d);
+        if (S.n > 0) {
+            cells += S.n;
+            rows += S.nt;
+            vals += (size_t)S.nt * S.n;
+        }
+    }
+    if (cells == 0) return APPFIS_GB_OK;
+    const size_t head = (sizeof(SrcDev) * MAXD + 255) / 256 * 256;
+    const size_t ibytes = (sizeof(int) * cells + 255) / 256 * 256;
+    std::vector<char> host(head + ibytes + sizeof(double) * (rows + vals));
+    void* dev;
+    GB_TRY(gb::workspace(gb::WS_FLOOD_SRC, host.size(), &dev));
+    SrcDev* tab = reinterpret_cast<SrcDev*>(host.data());
+    int* ci = reinterpret_cast<int*>(host.data() + head);
+    double* dv = reinterpret_cast<double*>(host.data() + head + ibytes);
+    char* base = reinterpret_cast<char*>(dev);
+    size_t oc = 0, od = 0;
+    for (int d = 0; d < MAXD; d++) tab[d] = SrcDev{0, 0, nullptr, nullptr, nullptr};
+    for (int d = 0; d < ndom; d++) {
+        const appfis_gb_flood_sources& S = srcs[d];
+        if (S.n <= 0) continue;
+        tab[d].n = S.n;
+        tab[d].nt = S.nt;
+        tab[d].cells = reinterpret_cast<const int*>(base + head) + oc;
+        std::memcpy(ci + oc, S.cells, sizeof(int) * S.n);
+        oc += S.n;
+        tab[d].times = reinterpret_cast<const double*>(base + head + ibytes) + od;
+        std::memcpy(dv + od, S.times, sizeof(double) * S.nt);
+        od += S.nt;
+        tab[d].flows = reinterpret_cast<const double*>(base + head + ibytes) + od;
+        std::memcpy(dv + od, S.flows, sizeof(double) * S.nt * S.n);
+        od += (size_t)S.nt * S.n;
+    }
+    GB_CUDA(cudaMemcpyAsync(dev, host.data(), host.size(), cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaStreamSynchronize(st));  // the host table is a local
+    *out = reinterpret_cast<const SrcDev*>(dev);
+    return APPFIS_GB_OK;
+}
+
 // Uploads the table, initialises the control block and launches the persistent kernel.
 template <class T>
 int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_params* prm, double* dev_dtlog, int* dev_steps,
-        double* dev_simtime, int* dev_status, cudaStream_t st)
+        double* dev_simtime, int* dev_status, cudaStream_t st, const appfis_gb_flood_sources* srcs = nullptr)
 {
     if (!doms || !prm || ndom < 1 || ndom > MAXD) return gb::fail(APPFIS_GB_EINVAL, "flood: 1..%d domains required", MAXD);
     if (!(prm->dx > 0) || !(prm->courant > 0) || !(prm->print_interval > 0) || prm->max_steps < 0)
@@ -140,6 +199,14 @@ int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_para
     p.total_strips = total;
     p.dtlog = prm->max_steps > 0 ? dev_dtlog : nullptr;
     p.zc = nullptr;
+    p.spin_limit = SPIN_LIMIT;
+    p.stall_cta = -1;
+    GB_TRY(upload_sources(doms, srcs, ndom, &p.srcs, st));
+    unsigned long long test_limit = 0;
+    if (gb::take_test_stall(gb::TEST_FLOOD_BARRIER, &test_limit)) {  // a test runs a barrier wait out
+        p.spin_limit = test_limit;
+        p.stall_cta = 0;
+    }
     if (prm->flags & APPFIS_GB_FLOOD_SKIP_DRY) {
         void* z;
         GB_TRY(gb::workspace(gb::WS_FLOOD_Z, 2 * (size_t)total, &z));

@@ -13,6 +13,21 @@ namespace gb {
 
 static thread_local std::string t_last_error;
 
+namespace {
+std::mutex g_test_mu;
+int g_test_kind = TEST_NONE;
+unsigned long long g_test_limit = 0;
+}  // namespace
+
+bool take_test_stall(int kind, unsigned long long* limit)
+{
+    std::lock_guard<std::mutex> lk(g_test_mu);
+    if (g_test_kind != kind) return false;
+    *limit = g_test_limit;
+    g_test_kind = TEST_NONE;
+    return true;
+}
+
 int fail(int code, const char* fmt, ...)
 {
     char buf[512];
@@ -185,6 +200,20 @@ int appfis_gb_stream_sync(void* stream)
 {
     GB_CUDA(cudaStreamSynchronize(gb::as_stream(stream)));
     return gb::check_status("appfis_gb_stream_sync");
+}
+
+int appfis_gb_test_stall_next(int kind, unsigned long long limit)
+{
+    if (kind != gb::TEST_NONE && kind != gb::TEST_FLOOD_BARRIER && kind != gb::TEST_TMA_SHORTFALL)
+        return gb::fail(APPFIS_GB_EINVAL, "test_stall_next: kind %d", kind);
+    if (kind == gb::TEST_FLOOD_BARRIER && (limit < 1 || limit > (1ull << 20)))
+        return gb::fail(APPFIS_GB_EINVAL, "test_stall_next: barrier poll limit %llu (1 .. 2^20)", limit);
+    if (kind == gb::TEST_TMA_SHORTFALL && (limit < 1000 || limit > 100000000ull))
+        return gb::fail(APPFIS_GB_EINVAL, "test_stall_next: wait limit %llu ns (1 us .. 100 ms)", limit);
+    std::lock_guard<std::mutex> lk(gb::g_test_mu);
+    gb::g_test_kind = kind;
+    gb::g_test_limit = limit;
+    return APPFIS_GB_OK;
 }
 
 }  // extern "C"

@@ -378,10 +378,14 @@ template <> __device__ __forceinline__ void stgv<__half, 2>(__half* p, const flo
     *reinterpret_cast<__half2*>(p) = __floats2half2_rn(r[0], r[1]);
 }
 
+// Waits: `wait_ns` per mbarrier wait (1 s in production); `shortfall` (testing only, 0 in
+// production) arms the first plane's barrier with that many bytes more than its copy delivers,
+// so that its wait runs out.
 template <class T, int MODE, int VXT>
 __global__ void __launch_bounds__(128, VXT == 4 ? 4 : 6) star_r4_tma(const __grid_constant__ CUtensorMap map, T* __restrict__ out,
                                                                      int nx, int ny, int nz, int px, int py, int kz, float coeff,
-                                                                     StarW wt, unsigned* __restrict__ status)
+                                                                     StarW wt, unsigned* __restrict__ status,
+                                                                     unsigned long long wait_ns, unsigned shortfall)
 {
     namespace f2 = gb::f2;
     typedef TmaStar<T, VXT> Lay;
@@ -410,10 +414,10 @@ __global__ void __launch_bounds__(128, VXT == 4 ? 4 : 6) star_r4_tma(const __gri
     auto issue = [&](int pl) {
         last_issued = pl;
         const int n = (pl - pbase) % TNS;
-        gb::tma::arrive_expect(&bar[n], Lay::BOX);
+        gb::tma::arrive_expect(&bar[n], Lay::BOX + (pl == pbase ? shortfall : 0u));
         gb::tma::load_3d(tsm + n * Lay::SLOT, &map, bx0, by0, pl, &bar[n]);
     };
-    auto ready = [&](int pl, uint64_t limit = 1000000000ull) {
+    auto ready = [&](int pl, uint64_t limit) {
         return gb::tma::wait(&bar[(pl - pbase) % TNS], (unsigned)((pl - pbase) / TNS) & 1u, limit);
     };
     if (t == 0)
@@ -424,7 +428,7 @@ __global__ void __launch_bounds__(128, VXT == 4 ? 4 : 6) star_r4_tma(const __gri
     VecN<VXT> q[TRY][9];
 #pragma unroll
     for (int m = 0; m < 8; m++) {  // planes k0-4 .. k0+3
-        if (!bad && !ready(pbase + m)) bad = true;
+        if (!bad && !ready(pbase + m, wait_ns)) bad = true;
 #pragma unroll
         for (int r = 0; r < TRY; r++) q[r][m] = ldsv<T, VXT>(slot(pbase + m) + own + r * SW);
     }
@@ -438,7 +442,7 @@ __global__ void __launch_bounds__(128, VXT == 4 ? 4 : 6) star_r4_tma(const __gri
         for (int P = 0; P < 9; P++) {
             const int k = kb + P;
             if (k < k1 && !bad) {
-                if (!ready(k + R)) bad = true;
+                if (!ready(k + R, wait_ns)) bad = true;
 #pragma unroll
                 for (int r = 0; r < TRY; r++) q[r][(P + 8) % 9] = ldsv<T, VXT>(slot(k + R) + own + r * SW);
                 const T* rowp = slot(k) + own;
@@ -570,9 +574,17 @@ int run_star_tma(T** buf, int nx, int ny, int nz, int pitch, int iters, int mode
                              (long long)per_sm * gb::sm_count(), 2 * R);
     }
     dim3 blk(16, TTY / TRY), grd(gb::ceil_div(nx, Lay::TX), gb::ceil_div(ny, TTY), gb::ceil_div(nz, tkz));
+    unsigned long long wait_ns = 1000000000ull, test_ns = 0;
+    unsigned shortfall = 0;
+    if (iters > 0 && gb::take_test_stall(gb::TEST_TMA_SHORTFALL, &test_ns)) {  // a test runs the first launch's waits out
+        wait_ns = test_ns;
+        shortfall = 16;
+    }
     int ci = 0;
     for (int it = 0; it < iters; it++) {
-        kern<<<grd, blk, smem, st>>>(maps[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2 * R, tkz, coeff, w, status);
+        kern<<<grd, blk, smem, st>>>(maps[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2 * R, tkz, coeff, w, status, wait_ns, shortfall);
+        wait_ns = 1000000000ull;
+        shortfall = 0;
         ci = 1 - ci;
     }
     GB_TRY(gb::launched("star_r4_tma"));

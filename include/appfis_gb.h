@@ -65,6 +65,20 @@ APPFIS_GB_API int appfis_gb_version(void);
  * that launch are then invalid): returns APPFIS_GB_ETIMEOUT if it was set. */
 APPFIS_GB_API int appfis_gb_stream_sync(void* stream);
 
+/* Testing the bounded device-side waits (no counterpart in the reference, which has none): makes
+ * the NEXT call of one kind run a wait out on purpose, so that a test can check that the call
+ * ends with APPFIS_GB_ETIMEOUT and that the device stays usable.  Nothing faults or hangs: every
+ * wait involved has a limit.  The plan applies to one call and is then cleared.
+ *  kind 1: the next appfis_gb_flood_run / _job: CTA 0 does not arrive at the first grid
+ *          barrier, and every barrier wait gives up after `limit` polls (1 .. 2^20; each poll
+ *          sleeps ~64 ns): the run stops, its status is APPFIS_GB_ETIMEOUT.
+ *  kind 2: the next TMA-staged radius-4 star launch (appfis_gb_star_r4): every CTA arms its
+ *          first plane's mbarrier for 16 bytes more than the copy delivers, and waits at most
+ *          `limit` ns (1e3 .. 1e8) per wait: the launch gives up, lets its copies land, and the
+ *          next appfis_gb_stream_sync returns APPFIS_GB_ETIMEOUT.
+ *  kind 0: clears a pending plan. */
+APPFIS_GB_API int appfis_gb_test_stall_next(int kind, unsigned long long limit);
+
 /* ----------------------------------------------------------------------------- reductions */
 /* Execute{1,2,3}DReduce over a box (Appfis/Runtime.hpp:225-255 dispatch; GPU path
  * Appfis/Runtime_CUDA.hpp:554-740; CPU path Runtime.hpp:597-913; AllReduce Communication.hpp:752-789).
@@ -241,7 +255,7 @@ APPFIS_GB_API int appfis_gb_star_r4_f64(double* a, double* b, int nx, int ny, in
  * Manning friction, HaloExchange, wet/dry fix) for a BATCH of independent domains of uneven
  * sizes advanced in one persistent cooperative launch, each domain with its own dt, simulated
  * time and step count, until every domain reaches t_end (or max_steps).  Point sources
- * (:352-373) are not part of this entry point.
+ * (:352-373): appfis_gb_flood_run_sources below.
  * A domain: padded (nx+2) x (ny+2) fields with row pitch `pitch`, element type `dtype`
  * (APPFIS_GB_F32 or APPFIS_GB_F64): h/qx/qy[0] = state at t_start, h/qx/qy[1] = second buffers
  * with the same ghost ring (0); dem with its ghost ring at the wall height (the reference uses
@@ -285,6 +299,24 @@ typedef struct {
 APPFIS_GB_API int appfis_gb_flood_run(const appfis_gb_flood_domain* doms, int ndom, int dtype,
                                       const appfis_gb_flood_params* prm, double* dev_dtlog, int* dev_steps,
                                       double* dev_simtime, int* dev_status, void* stream);
+/* Point sources of one domain (the reference's hydrograph inflows, Triton/src/triton_appfis.hpp:
+ * 218-293 set-up, 352-373 row search, 1115-1141 the Execute1D source functor): after every
+ * step's update, before the wet/dry fix, h at each source cell grows by flow * dt / dx^2 with
+ * flow interpolated in the hydrograph at the step's start time.  HOST arrays (copied per run):
+ * cells[n] = the reference's padded sub-grid index row * (nx + 2) + col of an interior cell;
+ * times[nt] in seconds, increasing; flows[nt * n] in m^3/s, row t holding the n sources at
+ * times[t].  n = 0: no sources in that domain. */
+typedef struct {
+    int n, nt;
+    const int* cells;
+    const double* times;
+    const double* flows;
+} appfis_gb_flood_sources;
+
+/* appfis_gb_flood_run with point sources: srcs[ndom] (one table per domain, n may be 0). */
+APPFIS_GB_API int appfis_gb_flood_run_sources(const appfis_gb_flood_domain* doms, const appfis_gb_flood_sources* srcs, int ndom,
+                                              int dtype, const appfis_gb_flood_params* prm, double* dev_dtlog, int* dev_steps,
+                                              double* dev_simtime, int* dev_status, void* stream);
 /* Initialises one domain's buffers (both state buffers, dem with a 1e6 ghost ring as the reference's
  * dem.SetBoundary(1e6), n2 = manning^2 everywhere) from FP64 DEVICE interiors dem, h, qx, qy
  * (nx*ny each; qx/qy may be NULL = 0). */

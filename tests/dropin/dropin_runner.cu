@@ -11,6 +11,12 @@
 //        dropin_runner fdtd   NX NY NZ ITERS COEFF in.f32 out.f32
 //        dropin_runner triton NX NY DX CN HEXTRA MANN T_END PRINT TSTEP MAXSTEPS dem.f64 h.f64 out.f64 dt.f64
 //        dropin_runner ireduce NX NY in.i32           (Execute2DReduce SUM / MAX / MIN of an int grid)
+//        dropin_runner ckpt NX NY G1 G2 in.u8 a.u8 b.u8 DIR [fast]
+//                      GameOfLife: G1 generations, SaveDeviceState, G2 more -> a; a second grid
+//                      restored with LoadDeviceState, G2 generations -> b (a == b == G1 + G2
+//                      generations); Array::Save/LoadBinaryFile round trip of the gathered grid
+// A trailing word routes the Execute loop to a hand-written kernel (APPFIS::UseFastKernel):
+//        heat2d ... fast | himeno ... fast | himeno ... mixed | fdtd ... fast | gol ... fast
 #include <cfloat>
 #include <cstdio>
 #include <cstdlib>
@@ -199,6 +205,16 @@ static void WriteFile(const char* path, const void* p, size_t bytes)
 	std::fclose(f);
 }
 
+// The trailing routing word at argv[at], if any.
+static APPFIS::FAST_KERNEL Routing(int argc, char** argv, int at, APPFIS::FAST_KERNEL fast)
+{
+	if (argc <= at) return APPFIS::FAST_NONE;
+	const std::string w(argv[at]);
+	if (w == "fast") return fast;
+	if (w == "mixed") return APPFIS::FAST_HIMENO_MIXED;
+	return APPFIS::FAST_NONE;
+}
+
 static int RunGol(int argc, char** argv)
 {
 	const int nx = std::atoi(argv[2]), ny = std::atoi(argv[3]), gens = std::atoi(argv[4]);
@@ -214,6 +230,7 @@ static int RunGol(int argc, char** argv)
 	APPFIS::Scatter(g.GetFullGrid(), g.GetSubGrid());
 	APPFIS::Config<int> config(g);
 	config.GridsToUpdate(g);
+	APPFIS::UseFastKernel(config, Routing(argc, argv, 7, APPFIS::FAST_LIFE));
 	APPFIS::InitializeExecution(g);
 	APPFIS::Timer timer;
 	timer.Start("COMPUTE");
@@ -255,6 +272,7 @@ static int RunHeat2d(int argc, char** argv)
 	g.SetBoundary(APPFIS::UP, top);
 	APPFIS::Config<float> config(g);
 	config.GridsToUpdate(g);
+	APPFIS::UseFastKernel(config, Routing(argc, argv, 9, APPFIS::FAST_HEAT2D));
 	APPFIS::InitializeExecution(g);
 	for (int t = 0; t < iters; t++) APPFIS::Execute2D(config, r, r, g.GetSubGrid(), g.GetSubGridNext());
 	float mx = 0, mn = 0, sm = 0;
@@ -287,6 +305,7 @@ static int RunHimeno(int argc, char** argv)
 	for (int c = 0; c < 12; c++) gc[c]->GetSubGrid()->SetData(reinterpret_cast<float*>(coef.data()) + c * padded);
 	APPFIS::Config<float> config(gp);
 	config.GridsToUpdate(gp);
+	APPFIS::UseFastKernel(config, Routing(argc, argv, 10, APPFIS::FAST_HIMENO));
 	APPFIS::InitializeExecution(gp, *gc[0], *gc[1], *gc[2], *gc[3], *gc[4], *gc[5], *gc[6], *gc[7], *gc[8], *gc[9], *gc[10], *gc[11]);
 	for (int t = 0; t < iters; t++)
 		APPFIS::Execute3D(config, omega, gc[0]->GetSubGrid(), gc[1]->GetSubGrid(), gc[2]->GetSubGrid(), gc[3]->GetSubGrid(),
@@ -317,6 +336,7 @@ static int RunFdtd(int argc, char** argv)
 	APPFIS::Scatter(g.GetFullGrid(), g.GetSubGrid());
 	APPFIS::Config<float> config(g);
 	config.GridsToUpdate(g);
+	APPFIS::UseFastKernel(config, Routing(argc, argv, 9, APPFIS::FAST_STAR_R4));
 	APPFIS::InitializeExecution(g);
 	for (int t = 0; t < iters; t++) APPFIS::Execute3D(config, coeff, radius, g.GetSubGrid(), g.GetSubGridNext());
 	APPFIS::FinalizeExecution(g);
@@ -428,6 +448,64 @@ static int RunIntReduce(int argc, char** argv)
 	return 0;
 }
 
+static void GolRun(APPFIS::Config<int>& config, APPFIS::Grid<int>& g, int gens)
+{
+	for (int t = 0; t < gens; t++) APPFIS::Execute2D(config, g.GetSubGrid(), g.GetSubGridNext());
+}
+
+static std::vector<unsigned char> GolInterior(APPFIS::Grid<int>& g, int nx, int ny)
+{
+	APPFIS::Gather(g.GetFullGrid(), g.GetSubGrid());
+	std::vector<unsigned char> out((size_t)nx * ny);
+	for (int j = 0; j < ny; j++)
+		for (int i = 0; i < nx; i++) out[(size_t)j * nx + i] = (unsigned char)g.GetFullGrid()->Get(i, j);
+	return out;
+}
+
+// Checkpoint / restart through the device state, and the host binary-file round trip.
+static int RunCheckpoint(int argc, char** argv)
+{
+	const int nx = std::atoi(argv[2]), ny = std::atoi(argv[3]), g1 = std::atoi(argv[4]), g2 = std::atoi(argv[5]);
+	std::vector<char> in = ReadFile(argv[6], (size_t)nx * ny);
+	const std::string dir(argv[9]);
+	const APPFIS::FAST_KERNEL route = Routing(argc, argv, 10, APPFIS::FAST_LIFE);
+	APPFIS::Attribute attr;
+	attr.ghostLayer = 1;
+	attr.periodic = true;
+	APPFIS::Initialize(argc, argv, APPFIS::DIM_2D, APPFIS::DIM_2D, attr);
+	APPFIS::Grid<int> g(APPFIS::DIM_2D, nx, ny, APPFIS::DUAL), h(APPFIS::DIM_2D, nx, ny, APPFIS::DUAL);
+	g.AllocateFullGrid();
+	h.AllocateFullGrid();
+	for (int j = 0; j < ny; j++)
+		for (int i = 0; i < nx; i++) g.GetFullGrid()->Set(i, j, (int)(unsigned char)in[(size_t)j * nx + i]);
+	APPFIS::Scatter(g.GetFullGrid(), g.GetSubGrid());
+	APPFIS::Config<int> cg(g), ch(h);
+	cg.GridsToUpdate(g);
+	ch.GridsToUpdate(h);
+	APPFIS::UseFastKernel(cg, route);
+	APPFIS::UseFastKernel(ch, route);
+	APPFIS::InitializeExecution(g, h);
+	GolRun(cg, g, g1);
+	APPFIS::SaveDeviceState(g, dir + "/state.bin");
+	GolRun(cg, g, g2);
+	APPFIS::LoadDeviceState(h, dir + "/state.bin");
+	GolRun(ch, h, g2);
+	APPFIS::FinalizeExecution(g, h);
+	std::vector<unsigned char> a = GolInterior(g, nx, ny), b = GolInterior(h, nx, ny);
+	WriteFile(argv[7], a.data(), a.size());
+	WriteFile(argv[8], b.data(), b.size());
+	// host binary files: the gathered grid written and read back
+	g.GetFullGrid()->SaveBinaryFile(dir + "/full.bin");
+	APPFIS::Array<int> back(APPFIS::DIM_2D, nx, ny);
+	back.LoadBinaryFile(dir + "/full.bin");
+	bool same = true;
+	for (int j = 0; j < ny && same; j++)
+		for (int i = 0; i < nx && same; i++) same = back.Get(i, j) == g.GetFullGrid()->Get(i, j);
+	std::printf("{\"binary_roundtrip\": %s}\n", same ? "true" : "false");
+	APPFIS::Finalize();
+	return 0;
+}
+
 int main(int argc, char** argv)
 {
 	if (argc < 2) return 2;
@@ -438,6 +516,7 @@ int main(int argc, char** argv)
 	if (mode == "fdtd") return RunFdtd(argc, argv);
 	if (mode == "triton") return RunTriton(argc, argv);
 	if (mode == "ireduce") return RunIntReduce(argc, argv);
+	if (mode == "ckpt") return RunCheckpoint(argc, argv);
 	std::fprintf(stderr, "unknown mode %s\n", argv[1]);
 	return 2;
 }

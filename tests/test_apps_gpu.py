@@ -143,3 +143,87 @@ def test_fast_kernel_fdtd_field_matches_reference(exes, fast_exes, tmp_path, dim
         texts[name] = (d / "output" / "output.txt").read_text()
     assert len(texts["ref"]) > 1000
     assert texts["fast"] == texts["ref"]
+
+
+def test_triton_application_restart_from_checkpoint_files(exes, tmp_path):
+    """The Triton application's restart path (Triton/src/config_utils.hpp:369-379,
+    triton_appfis.hpp:158-213,311-312): a run to t = 60 s writes h/u/v; a second run starts from
+    those files (h_infile, qx_infile, qy_infile, sim_start_time = 60, checkpoint_id = 1,
+    it_count = the first run's steps) and continues to 120 s.  The drop-in build and the
+    reference's CPU build restart from the same files and must agree like the plain runs."""
+    import shutil
+    gbx, ref = exes
+    nx, ny, seed = 64, 48, 21
+    first = tmp_path / "first"
+    first.mkdir()
+    W.write_triton_case(str(first), nx, ny, seed, 60)
+    text = run(ref["Triton"], ["case.cfg", "-output", "-thread=4"], str(first))
+    n1 = int(re.search(r"^Number of iteration:\s*(\d+)", text, re.M).group(1))
+    out = {}
+    for name, exe, extra in (("gb", gbx["Triton"], []), ("ref", ref["Triton"], ["-thread=4"])):
+        d = tmp_path / name
+        d.mkdir()
+        W.write_triton_case(str(d), nx, ny, seed, 120)
+        for f in ("h", "u", "v"):
+            shutil.copy(str(first / "output" / ("%s.txt" % f)), str(d / ("%s0.txt" % f)))
+        cfg = (d / "case.cfg").read_text().replace("h_infile=h.asc", "h_infile=h0.txt")
+        cfg = cfg.replace("sim_start_time=0", "sim_start_time=60")
+        cfg += "qx_infile=u0.txt\nqy_infile=v0.txt\ncheckpoint_id=1\nit_count=%d\n" % n1
+        (d / "case.cfg").write_text(cfg)
+        text = run(exe, ["case.cfg", "-output"] + extra, str(d))
+        steps = int(re.search(r"^Number of iteration:\s*(\d+)", text, re.M).group(1))
+        out[name] = (steps, [np.loadtxt(str(d / "output" / f)) for f in ("h.txt", "u.txt", "v.txt")])
+    assert out["gb"][0] == out["ref"][0] > n1  # the count continues from it_count
+    for a, b in zip(out["gb"][1], out["ref"][1]):
+        assert a.shape == (ny, nx)
+        assert np.abs(a - b).max() <= 2e-6
+
+
+def test_batched_flood_point_source_matches_reference_application(exes, gb, torch_cuda, tmp_path):
+    """The batched persistent flood kernel with a point source (appfis_gb_flood_run_sources, FP64)
+    on the Triton application's own case files (DEM, initial depth, hydrograph converted from
+    hours, source location through the reference's cell formula, triton_appfis.hpp:218-237,
+    555-564) gives the reference CPU build's step count and h/u/v fields (6 printed decimals)."""
+    import ctypes
+    import math
+    from appfis_gb300 import _lib
+    torch = torch_cuda
+    _, ref = exes
+    nx, ny, seed, duration = 48, 40, 77, 120
+    W.write_triton_case(str(tmp_path), nx, ny, seed, duration)
+    text = run(ref["Triton"], ["case.cfg", "-output", "-thread=4"], str(tmp_path))
+    ref_steps = int(re.search(r"^Number of iteration:\s*(\d+)", text, re.M).group(1))
+    want = [np.loadtxt(str(tmp_path / "output" / f)) for f in ("h.txt", "u.txt", "v.txt")]
+    dem = np.loadtxt(str(tmp_path / "dem.asc"), skiprows=6)
+    h0 = np.loadtxt(str(tmp_path / "h.asc"))
+    rows = [l.split("%")[0].strip() for l in open(str(tmp_path / "hydro.txt"))]
+    hyd = np.array([[float(v) for v in r.split(",")] for r in rows if r])
+    sx, sy = [float(v) for v in [l for l in open(str(tmp_path / "src.txt")) if not l.startswith("%")][0].split(",")]
+    col, row = math.ceil(sx / 10.0) - 1, math.ceil(ny - sy / 10.0) - 1
+    cells = np.array([(row + 1) * (nx + 2) + (col + 1)], dtype=np.int32)
+    times = np.ascontiguousarray(hyd[:, 0] * 3600.0)
+    flows = np.ascontiguousarray(hyd[:, 1:])
+    srcs = (_lib.FloodSources * 1)()
+    srcs[0].n, srcs[0].nt = 1, len(times)
+    srcs[0].cells, srcs[0].times, srcs[0].flows = cells.ctypes.data, times.ctypes.data, flows.ctypes.data
+    pitch = (nx + 2 + 15) // 16 * 16
+    f = torch.zeros((8, ny + 2, pitch), dtype=torch.float64, device="cuda")
+    dom = (_lib.FloodDomain * 1)()
+    d = dom[0]
+    d.nx, d.ny, d.pitch = nx, ny, pitch
+    d.h[0], d.h[1], d.qx[0], d.qx[1], d.qy[0], d.qy[1] = [f[m].data_ptr() for m in range(6)]
+    d.dem, d.n2 = f[6].data_ptr(), f[7].data_ptr()
+    dd, hh = torch.from_numpy(dem).cuda(), torch.from_numpy(h0).cuda()
+    gb.call("appfis_gb_flood_setup", ctypes.byref(d), _lib.F64, dd.data_ptr(), hh.data_ptr(), None, None, 0.035, None)
+    prm = _lib.FloodParams(10.0, 0.5, 1e-3, float(duration), 60.0, 1.0, 0.0, 0)
+    steps = torch.zeros(1, dtype=torch.int32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    gb.call("appfis_gb_flood_run_sources", dom, srcs, 1, _lib.F64, ctypes.byref(prm), None, steps.data_ptr(), None,
+            status.data_ptr(), None)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0 and int(steps.item()) == ref_steps
+    b = int(steps.item()) & 1
+    got = [f[2 * k + b][1:ny + 1, 1:nx + 1].cpu().numpy() for k in range(3)]
+    assert got[0].sum() > h0.sum()  # the source added water
+    for a, w in zip(got, want):
+        assert np.abs(a - w).max() <= 2e-6
