@@ -277,13 +277,13 @@ namespace APPFIS
 		inline unsigned Blocks(int n, int b) { return (unsigned)((n + b - 1) / b); }
 
 		template<class T>
-		void RefreshGhosts(Grid<T>* g, bool next)
+		void RefreshGhosts(Grid<T>* g, bool next, cudaStream_t st = nullptr)
 		{
 			if (GetGhostLayer() <= 0 || !IsPeriodic() || g->GetGridType() == FLAT) return;
 			Array<T>* a = next ? g->GetSubGridNextCPU() : g->GetSubGridCPU();
 			const int d[3] = { a->GetDim(0), a->GetDim(1), a->GetDim(2) };
 			Check(appfis_gb_ghost_periodic(next ? g->DeviceNext() : g->DeviceCurrent(), (int)sizeof(T), a->GetDimCount(), d,
-				GetGhostLayer(), GetCudaStream()), "periodic ghost refresh");
+				GetGhostLayer(), st ? st : GetCudaStream()), "periodic ghost refresh");
 		}
 
 		// After a sweep: refresh the updated grids' next buffers, then swap them in.
@@ -335,17 +335,216 @@ namespace APPFIS
 		FinalizeExecution(args...);
 	}
 
+	namespace detail
+	{
+		// The functor over the box [x0, x1) x [y0, y1) on `st` (no ghost refresh, no swap).
+		template<typename... TArgs>
+		void Sweep2D(int x0, int x1, int y0, int y1, cudaStream_t st, TArgs... args)
+		{
+			if (x1 <= x0 || y1 <= y0) return;
+			constexpr int M = ArrayCount<typename KArg<TArgs>::type...>::value <= MARCH_MAX_ARRAYS_2D ? MARCH : 1;
+			dim3 blk(32, 8), grd(Blocks(x1 - x0, 32), Blocks(y1 - y0, 8 * M));
+			Shape s;
+			const bool uniform = UniformShape(s, args...);
+			const long long rows = (y1 - y0 + M - 1) / M, n = (long long)(x1 - x0) * rows;
+			if (uniform && Flatten(x1 - x0, M, n, 1))
+				Functor2DF<M, typename KArg<TArgs>::type...><<<Blocks((int)n, 256), 256, 0, st>>>(
+					x0, y0, y1, (unsigned)n, MakeDiv(x1 - x0), s, KArg<TArgs>::to(args)...);
+			else if (uniform)
+				Functor2DU<M, typename KArg<TArgs>::type...><<<grd, blk, 0, st>>>(x0, x1, y0, y1, s, KArg<TArgs>::to(args)...);
+			else
+				Functor2D<M, typename KArg<TArgs>::type...><<<grd, blk, 0, st>>>(x0, x1, y0, y1, KArg<TArgs>::to(args)...);
+		}
+
+		// The functor over the box [x0, x1) x [y0, y1) x [z0, z1) on `st`.
+		template<typename... TArgs>
+		void Sweep3D(int x0, int x1, int y0, int y1, int z0, int z1, cudaStream_t st, TArgs... args)
+		{
+			if (x1 <= x0 || y1 <= y0 || z1 <= z0) return;
+			Shape s;
+			const bool uniform = UniformShape(s, args...);
+			const long long plane = (long long)(x1 - x0) * (y1 - y0);
+			if (ArrayCount<typename KArg<TArgs>::type...>::value <= MARCH_MAX_ARRAYS)
+			{
+				dim3 blk(32, 8, 1), grd(Blocks(x1 - x0, 32), Blocks(y1 - y0, 8), Blocks(z1 - z0, MARCH_3D));
+				if (uniform && Flatten(x1 - x0, MARCH_3D, plane, grd.z))
+					Functor3DF<MARCH_3D, typename KArg<TArgs>::type...><<<dim3(Blocks((int)plane, 256), grd.z), 256, 0, st>>>(
+						x0, y0, z0, z1, (unsigned)plane, MakeDiv(x1 - x0), s, KArg<TArgs>::to(args)...);
+				else if (uniform)
+					Functor3DU<MARCH_3D, typename KArg<TArgs>::type...><<<grd, blk, 0, st>>>(x0, x1, y0, y1, z0, z1, s,
+						KArg<TArgs>::to(args)...);
+				else
+					Functor3D<MARCH_3D, typename KArg<TArgs>::type...><<<grd, blk, 0, st>>>(x0, x1, y0, y1, z0, z1,
+						KArg<TArgs>::to(args)...);
+			}
+			else
+			{
+				dim3 blk(32, 4, 2), grd(Blocks(x1 - x0, 32), Blocks(y1 - y0, 4), Blocks(z1 - z0, 2));
+				if (uniform && Flatten(x1 - x0, 1, plane, z1 - z0))
+					Functor3DF<1, typename KArg<TArgs>::type...><<<dim3(Blocks((int)plane, 256), z1 - z0), 256, 0, st>>>(
+						x0, y0, z0, z1, (unsigned)plane, MakeDiv(x1 - x0), s, KArg<TArgs>::to(args)...);
+				else if (uniform)
+					Functor3DU<1, typename KArg<TArgs>::type...><<<grd, blk, 0, st>>>(x0, x1, y0, y1, z0, z1, s, KArg<TArgs>::to(args)...);
+				else
+					Functor3D<1, typename KArg<TArgs>::type...><<<grd, blk, 0, st>>>(x0, x1, y0, y1, z0, z1, KArg<TArgs>::to(args)...);
+			}
+		}
+
+		// The overlapped form (the reference's ExecuteOverlap*, Appfis/Runtime.hpp:372-594,
+		// Runtime_CUDA.hpp:304-551: the boundary strips first, the halo exchange behind the
+		// interior).  On one GPU the exchange is the periodic ghost refresh of the updated grids'
+		// next buffers; it reads only the strips of width `ghost` along the box's faces, so it runs
+		// on a second stream while the interior [2 ghost, dim - 2 ghost) is swept.  Applies when the
+		// grids are periodic and the Config box is the whole interior with room for both parts.
+		struct OverlapLane
+		{
+			cudaStream_t side = nullptr;
+			cudaEvent_t strips = nullptr, halo = nullptr;
+		};
+
+		inline OverlapLane& Overlap()
+		{
+			static OverlapLane o;
+			if (!o.side)
+			{
+				CheckCuda(cudaStreamCreateWithFlags(&o.side, cudaStreamNonBlocking), "cudaStreamCreate(overlap)");
+				CheckCuda(cudaEventCreateWithFlags(&o.strips, cudaEventDisableTiming), "cudaEventCreate(overlap)");
+				CheckCuda(cudaEventCreateWithFlags(&o.halo, cudaEventDisableTiming), "cudaEventCreate(overlap)");
+			}
+			return o;
+		}
+
+		template<class T>
+		bool Overlappable(Config<T>& config, int nDim)
+		{
+			const int g = GetGhostLayer();
+			if (!IsPeriodic() || g <= 0 || config.updatedGrids.empty()) return false;
+			const int s[3] = { config.GetStartX(), config.GetStartY(), config.GetStartZ() };
+			const int e[3] = { config.GetEndX(), config.GetEndY(), config.GetEndZ() };
+			const int d[3] = { config.GetDimX(), config.GetDimY(), config.GetDimZ() };
+			for (int a = 0; a < nDim; a++)
+				if (s[a] != g || e[a] != d[a] - g || d[a] < 5 * g) return false;
+			return true;
+		}
+
+		// Strips swept: refresh the updated grids' next ghosts on the side stream, behind the interior.
+		template<class T>
+		void OverlapHalo(Config<T>& config)
+		{
+			OverlapLane& o = Overlap();
+			CheckCuda(cudaEventRecord(o.strips, GetCudaStream()), "overlap event");
+			CheckCuda(cudaStreamWaitEvent(o.side, o.strips, 0), "overlap wait");
+			for (size_t n = 0; n < config.updatedGrids.size(); n++) RefreshGhosts(config.updatedGrids[n], true, o.side);
+			CheckCuda(cudaEventRecord(o.halo, o.side), "overlap event");
+		}
+
+		template<class T>
+		void OverlapJoin(Config<T>& config)
+		{
+			Check(gb_launch_status(), "stencil kernel launch");
+			CheckCuda(cudaStreamWaitEvent(GetCudaStream(), Overlap().halo, 0), "overlap wait");
+			for (size_t n = 0; n < config.updatedGrids.size(); n++) config.updatedGrids[n]->Swap();
+		}
+
+		template<typename T, typename... TArgs>
+		bool Routed(Config<T>& config, TArgs... args)
+		{
+			FastState* fs = FastFind(&config);
+			if (!fs)
+			{
+				FlushFast();  // a functor sweep reads the grids as the deferred sweeps leave them
+				return false;
+			}
+			FlushFast(fs);
+			FastCall(*fs, config, args...);
+			FastAfter(config);
+			return true;
+		}
+	}
+
+	// Overlapped executors (also what Execute*D runs when the Attribute asks for overlap, as the
+	// reference's Execute*DGPU do: Runtime_CUDA.hpp:231-276); outside their conditions (above)
+	// they are the plain sweeps.
+	template<typename T, typename... TArgs>
+	void ExecuteOverlap1D(Config<T>& config, TArgs... args)
+	{
+		if (detail::Routed(config, args...)) return;
+		const int g = GetGhostLayer(), x0 = config.GetStartX(), x1 = config.GetEndX();
+		if (!detail::Overlappable(config, 1))
+		{
+			if (x1 > x0)
+				detail::Functor1D<typename detail::KArg<TArgs>::type...><<<detail::Blocks(x1 - x0, 256), 256, 0, GetCudaStream()>>>(
+					x0, x1, detail::KArg<TArgs>::to(args)...);
+			detail::AfterSweep(config);
+			return;
+		}
+		cudaStream_t st = GetCudaStream();
+		detail::Functor1D<typename detail::KArg<TArgs>::type...><<<detail::Blocks(g, 256), 256, 0, st>>>(x0, 2 * g,
+			detail::KArg<TArgs>::to(args)...);
+		detail::Functor1D<typename detail::KArg<TArgs>::type...><<<detail::Blocks(g, 256), 256, 0, st>>>(x1 - g, x1,
+			detail::KArg<TArgs>::to(args)...);
+		detail::OverlapHalo(config);
+		detail::Functor1D<typename detail::KArg<TArgs>::type...><<<detail::Blocks(x1 - x0 - 2 * g, 256), 256, 0, st>>>(2 * g, x1 - g,
+			detail::KArg<TArgs>::to(args)...);
+		detail::OverlapJoin(config);
+	}
+
+	template<typename T, typename... TArgs>
+	void ExecuteOverlap2D(Config<T>& config, TArgs... args)
+	{
+		if (detail::Routed(config, args...)) return;
+		const int x0 = config.GetStartX(), x1 = config.GetEndX(), y0 = config.GetStartY(), y1 = config.GetEndY();
+		cudaStream_t st = GetCudaStream();
+		if (!detail::Overlappable(config, 2))
+		{
+			detail::Sweep2D(x0, x1, y0, y1, st, args...);
+			detail::AfterSweep(config);
+			return;
+		}
+		const int g = GetGhostLayer();
+		detail::Sweep2D(x0, x1, y0, y0 + g, st, args...);          // strips along the y faces (full x)
+		detail::Sweep2D(x0, x1, y1 - g, y1, st, args...);
+		detail::Sweep2D(x0, x0 + g, y0 + g, y1 - g, st, args...);  // strips along the x faces
+		detail::Sweep2D(x1 - g, x1, y0 + g, y1 - g, st, args...);
+		detail::OverlapHalo(config);
+		detail::Sweep2D(x0 + g, x1 - g, y0 + g, y1 - g, st, args...);  // interior, behind the refresh
+		detail::OverlapJoin(config);
+	}
+
+	template<typename T, typename... TArgs>
+	void ExecuteOverlap3D(Config<T>& config, TArgs... args)
+	{
+		if (detail::Routed(config, args...)) return;
+		const int x0 = config.GetStartX(), x1 = config.GetEndX(), y0 = config.GetStartY(), y1 = config.GetEndY();
+		const int z0 = config.GetStartZ(), z1 = config.GetEndZ();
+		cudaStream_t st = GetCudaStream();
+		if (!detail::Overlappable(config, 3))
+		{
+			detail::Sweep3D(x0, x1, y0, y1, z0, z1, st, args...);
+			detail::AfterSweep(config);
+			return;
+		}
+		const int g = GetGhostLayer();
+		detail::Sweep3D(x0, x1, y0, y1, z0, z0 + g, st, args...);                  // z faces (full x, y)
+		detail::Sweep3D(x0, x1, y0, y1, z1 - g, z1, st, args...);
+		detail::Sweep3D(x0, x1, y0, y0 + g, z0 + g, z1 - g, st, args...);          // y faces (full x)
+		detail::Sweep3D(x0, x1, y1 - g, y1, z0 + g, z1 - g, st, args...);
+		detail::Sweep3D(x0, x0 + g, y0 + g, y1 - g, z0 + g, z1 - g, st, args...);  // x faces
+		detail::Sweep3D(x1 - g, x1, y0 + g, y1 - g, z0 + g, z1 - g, st, args...);
+		detail::OverlapHalo(config);
+		detail::Sweep3D(x0 + g, x1 - g, y0 + g, y1 - g, z0 + g, z1 - g, st, args...);
+		detail::OverlapJoin(config);
+	}
+
 	template<typename T, typename... TArgs>
 	void Execute1D(Config<T>& config, TArgs... args)
 	{
-		if (detail::FastState* fs = detail::FastFind(&config))  // routed by UseFastKernel
+		if (IsOverlap())
 		{
-			detail::FlushFast(fs);
-			detail::FastCall(*fs, config, args...);
-			detail::FastAfter(config);
+			ExecuteOverlap1D(config, args...);
 			return;
 		}
-		detail::FlushFast();  // a functor sweep reads the grids as the deferred sweeps leave them
+		if (detail::Routed(config, args...)) return;
 		const int x0 = config.GetStartX(), x1 = config.GetEndX();
 		if (x1 > x0)
 			detail::Functor1D<typename detail::KArg<TArgs>::type...><<<detail::Blocks(x1 - x0, 256), 256, 0, GetCudaStream()>>>(
@@ -356,97 +555,29 @@ namespace APPFIS
 	template<typename T, typename... TArgs>
 	void Execute2D(Config<T>& config, TArgs... args)
 	{
-		if (detail::FastState* fs = detail::FastFind(&config))  // routed by UseFastKernel
+		if (IsOverlap())
 		{
-			detail::FlushFast(fs);
-			detail::FastCall(*fs, config, args...);
-			detail::FastAfter(config);
+			ExecuteOverlap2D(config, args...);
 			return;
 		}
-		detail::FlushFast();  // a functor sweep reads the grids as the deferred sweeps leave them
-		const int x0 = config.GetStartX(), x1 = config.GetEndX(), y0 = config.GetStartY(), y1 = config.GetEndY();
-		if (x1 > x0 && y1 > y0)
-		{
-			constexpr int M =
-				detail::ArrayCount<typename detail::KArg<TArgs>::type...>::value <= detail::MARCH_MAX_ARRAYS_2D ? detail::MARCH : 1;
-			dim3 blk(32, 8), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 8 * M));
-			detail::Shape s;
-			const bool uniform = detail::UniformShape(s, args...);
-			const long long rows = (y1 - y0 + M - 1) / M, n = (long long)(x1 - x0) * rows;
-			if (uniform && detail::Flatten(x1 - x0, M, n, 1))
-				detail::Functor2DF<M, typename detail::KArg<TArgs>::type...><<<detail::Blocks((int)n, 256), 256, 0, GetCudaStream()>>>(
-					x0, y0, y1, (unsigned)n, detail::MakeDiv(x1 - x0), s, detail::KArg<TArgs>::to(args)...);
-			else if (uniform)
-				detail::Functor2DU<M, typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
-					x0, x1, y0, y1, s, detail::KArg<TArgs>::to(args)...);
-			else
-				detail::Functor2D<M, typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
-					x0, x1, y0, y1, detail::KArg<TArgs>::to(args)...);
-		}
+		if (detail::Routed(config, args...)) return;
+		detail::Sweep2D(config.GetStartX(), config.GetEndX(), config.GetStartY(), config.GetEndY(), GetCudaStream(), args...);
 		detail::AfterSweep(config);
 	}
 
 	template<typename T, typename... TArgs>
 	void Execute3D(Config<T>& config, TArgs... args)
 	{
-		if (detail::FastState* fs = detail::FastFind(&config))  // routed by UseFastKernel
+		if (IsOverlap())
 		{
-			detail::FlushFast(fs);
-			detail::FastCall(*fs, config, args...);
-			detail::FastAfter(config);
+			ExecuteOverlap3D(config, args...);
 			return;
 		}
-		detail::FlushFast();  // a functor sweep reads the grids as the deferred sweeps leave them
-		const int x0 = config.GetStartX(), x1 = config.GetEndX(), y0 = config.GetStartY(), y1 = config.GetEndY();
-		const int z0 = config.GetStartZ(), z1 = config.GetEndZ();
-		if (x1 > x0 && y1 > y0 && z1 > z0)
-		{
-			detail::Shape s;
-			const bool uniform = detail::UniformShape(s, args...);
-			const long long plane = (long long)(x1 - x0) * (y1 - y0);
-			if (detail::ArrayCount<typename detail::KArg<TArgs>::type...>::value <= detail::MARCH_MAX_ARRAYS)
-			{
-				dim3 blk(32, 8, 1), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 8), detail::Blocks(z1 - z0, detail::MARCH_3D));
-				if (uniform && detail::Flatten(x1 - x0, detail::MARCH_3D, plane, grd.z))
-					detail::Functor3DF<detail::MARCH_3D, typename detail::KArg<TArgs>::type...>
-						<<<dim3(detail::Blocks((int)plane, 256), grd.z), 256, 0, GetCudaStream()>>>(
-							x0, y0, z0, z1, (unsigned)plane, detail::MakeDiv(x1 - x0), s, detail::KArg<TArgs>::to(args)...);
-				else if (uniform)
-					detail::Functor3DU<detail::MARCH_3D, typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
-						x0, x1, y0, y1, z0, z1, s, detail::KArg<TArgs>::to(args)...);
-				else
-					detail::Functor3D<detail::MARCH_3D, typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
-						x0, x1, y0, y1, z0, z1, detail::KArg<TArgs>::to(args)...);
-			}
-			else
-			{
-				dim3 blk(32, 4, 2), grd(detail::Blocks(x1 - x0, 32), detail::Blocks(y1 - y0, 4), detail::Blocks(z1 - z0, 2));
-				if (uniform && detail::Flatten(x1 - x0, 1, plane, z1 - z0))
-					detail::Functor3DF<1, typename detail::KArg<TArgs>::type...>
-						<<<dim3(detail::Blocks((int)plane, 256), z1 - z0), 256, 0, GetCudaStream()>>>(
-							x0, y0, z0, z1, (unsigned)plane, detail::MakeDiv(x1 - x0), s, detail::KArg<TArgs>::to(args)...);
-				else if (uniform)
-					detail::Functor3DU<1, typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
-						x0, x1, y0, y1, z0, z1, s, detail::KArg<TArgs>::to(args)...);
-				else
-					detail::Functor3D<1, typename detail::KArg<TArgs>::type...><<<grd, blk, 0, GetCudaStream()>>>(
-						x0, x1, y0, y1, z0, z1, detail::KArg<TArgs>::to(args)...);
-			}
-		}
+		if (detail::Routed(config, args...)) return;
+		detail::Sweep3D(config.GetStartX(), config.GetEndX(), config.GetStartY(), config.GetEndY(), config.GetStartZ(),
+			config.GetEndZ(), GetCudaStream(), args...);
 		detail::AfterSweep(config);
 	}
-
-	// The reference's overlapped executors (Appfis/Runtime.hpp:372-594: boundary strips first, the
-	// halo exchange behind the interior) do the same sweep; with one rank per GPU there is no
-	// exchange to hide, so they are the plain executors.
-	template<typename T, typename... TArgs>
-	void ExecuteOverlap1D(Config<T>& config, TArgs... args) { Execute1D(config, args...); }
-
-	template<typename T, typename... TArgs>
-	void ExecuteOverlap2D(Config<T>& config, TArgs... args) { Execute2D(config, args...); }
-
-	template<typename T, typename... TArgs>
-	void ExecuteOverlap3D(Config<T>& config, TArgs... args) { Execute3D(config, args...); }
 
 	namespace detail
 	{

@@ -16,7 +16,7 @@ F32, F64, I32, F16 = 0, 1, 2, 3
 MAX, MIN, SUM = 0, 1, 2
 LIFE_REFERENCE, LIFE_B3S23 = 0, 1
 FORM_U8, FORM_BITS = 0, 1
-STAR_AUTO, STAR_SCALAR2, STAR_SCALAR4, STAR_TMA_X4, STAR_TMA_X2, STAR_VEC = 0, 2, 4, 8, 9, 10
+STAR_AUTO, STAR_SCALAR2, STAR_SCALAR4, STAR_TMA_X4, STAR_TMA_X2, STAR_VEC, STAR_TB2, STAR_TB2_8 = 0, 2, 4, 8, 9, 10, 11, 12
 
 _P = ctypes.c_void_p
 _i = ctypes.c_int
@@ -50,6 +50,7 @@ SIGNATURES = {
     "appfis_gb_himeno_mixed": [_P, _P, _P, _P, _i, _i, _i, _i, _i, _i, _f, _P, _P, _P],
     "appfis_gb_himeno_job": [_P, _P, _i, _i, _i, _i, _f, _i, _i, _P],
     "appfis_gb_star_r4": [_P, _P, _i, _i, _i, _i, _i, _i, _i, _f, _P, _i, _i, _P, _P],
+    "appfis_gb_star_r4_tune": [_P, _P, _i, _i, _i, _i, _i, _i, _f, _P, _P, _P, _P, _P],
     "appfis_gb_heat2d_f64": [_P, _P, _i, _i, _i, _i, _d, _d, _P, _P],
     "appfis_gb_himeno_f64": [_P, _P, _P, _i, _i, _i, _i, _i, _d, _P, _P, _P],
     "appfis_gb_star_r4_f64": [_P, _P, _i, _i, _i, _i, _i, _i, _d, _P, _P, _P],

@@ -714,6 +714,10 @@ def bench_himeno(torch, gb, W, dev, sp, hbm):
 
 
 def bench_fdtd(torch, gb, W, dev, sp, hbm):
+    """plain: the single-step FP32 TMA tile (the reference functor's data flow, one step per
+    launch).  Chosen forms: what the autotuner (appfis_gb_star_r4_tune) picks for FP32 and for
+    FP16 storage among the single-step tiles and the two-step time-blocked tiles, times z chunks;
+    each with its 200-step time, speed-up over plain and error against the FP64 form."""
     c = W.FDTD
     nx, ny, nz, it = c["nx"], c["ny"], c["nz"], c["iters"]
     w = (ctypes.c_float * 5)(*W.fdtd_weights())
@@ -723,25 +727,23 @@ def bench_fdtd(torch, gb, W, dev, sp, hbm):
     ha, hb = h0.clone(), h0.clone()
     ci = ctypes.c_int(0)
     res = {}
+    TMA_X4, AUTO = 8, 0
+    names = {8: "star_r4_tma (4 x points / thread)", 9: "star_r4_tma (2 x points / thread)", 10: "star_r4_vec",
+             11: "star_r4_tb2 (two steps per launch, 64 x 16)", 12: "star_r4_tb2 (two steps per launch, 64 x 8)"}
 
-    def run(x, y, x0, dt, iters):
+    def run(x, y, x0, dt, iters, tile):
         def f():
             x.copy_(x0)
-            gb.call("appfis_gb_star_r4", x.data_ptr(), y.data_ptr(), dt, nx, ny, nz, nx + 8, iters, 1, 0.0, w, 0, 0,
+            gb.call("appfis_gb_star_r4", x.data_ptr(), y.data_ptr(), dt, nx, ny, nz, nx + 8, iters, 1, 0.0, w, tile, 0,
                     ctypes.byref(ci), sp.cuda_stream)
         return f
-
-    lups = nx * ny * nz * it
-    ms32 = _time(torch, sp, run(a, b, f32, 0, it))
-    o32 = (a if ci.value == 0 else b).clone()
-    ms16 = _time(torch, sp, run(ha, hb, h0, 3, it))
-    o16 = (ha if ci.value == 0 else hb).float()
 
     def steps_only(x, y, dt, tile, n=10):  # n steps on the current state, no reset: kernel time per step
         one = lambda: gb.call("appfis_gb_star_r4", x.data_ptr(), y.data_ptr(), dt, nx, ny, nz, nx + 8, n, 1, 0.0, w, tile, 0,
                               ctypes.byref(ci), sp.cuda_stream)
         return _time(torch, sp, one, reps=1) / n
 
+    lups = nx * ny * nz * it
     # FP64 reference of the same 200 steps (appfis_gb_star_r4_f64, the weights in double)
     w64 = (ctypes.c_double * 5)(*W.fdtd_weights())
     x64 = f32.double()
@@ -749,26 +751,36 @@ def bench_fdtd(torch, gb, W, dev, sp, hbm):
     gb.call("appfis_gb_star_r4_f64", x64.data_ptr(), y64.data_ptr(), nx, ny, nz, nx + 8, it, 1, 0.0, w64, ctypes.byref(ci),
             sp.cuda_stream)
     r64 = x64 if ci.value == 0 else y64
-    err32, err16 = _err(o32, r64), _err(o16, r64)
-    del x64, y64, r64
-    s32 = steps_only(a, b, 0, 0)
-    s16 = steps_only(ha, hb, 3, 0)
-    # one step of each tile (APPFIS_GB_STAR_TMA_X4 / TMA_X2 / VEC), averaged over 10
-    tiles = {}
-    for tname, tid in (("tma_x4", 8), ("tma_x2", 9), ("vec", 10)):
-        for dname, x, y, dt in (("fp32", a, b, 0), ("fp16", ha, hb, 3)):
-            tiles["%s_%s_ms" % (tname, dname)] = steps_only(x, y, dt, tid)
+
+    ms32 = _time(torch, sp, run(a, b, f32, 0, it, TMA_X4))
+    err32 = _err((a if ci.value == 0 else b), r64)
+    s32 = steps_only(a, b, 0, TMA_X4)
     g32 = nx * ny * nz * 8 / (s32 * 1e-3) / 1e9
-    g16 = nx * ny * nz * 4 / (s16 * 1e-3) / 1e9
     res["workload"] = "fdtd3d radius-4 star 512^3, 200 steps of u <- u + 0.1*L8(u), zero halo of 4"
     res["plain_fp32"] = {"glups": lups / (ms32 * 1e-3) / 1e9, "ms": ms32, "bytes_per_lup": 8, "sweep_ms": s32,
                          "kernel": "star_r4_tma<float>", "achieved_gbs": g32, "frac_of_hbm": g32 / hbm,
                          "traffic": profiled_traffic("star_r4_tma<float>"), "error_vs_fp64": err32}
-    res["fp16_storage"] = {"glups": lups / (ms16 * 1e-3) / 1e9, "ms": ms16, "bytes_per_lup": 4, "sweep_ms": s16,
-                           "kernel": "star_r4_tma<half>", "achieved_gbs": g16, "frac_of_hbm": g16 / hbm,
-                           "traffic": profiled_traffic("star_r4_tma<half>"), "speedup_vs_plain": ms32 / ms16,
-                           "step_ms_by_tile": tiles,
-                           "max_abs_diff_vs_fp32": float((o16 - o32).abs().max().item()), "error_vs_fp64": err16}
+    # one step of every tile (10 steps each, per-step time)
+    tiles = {}
+    for tname, tid in (("tma_x4", 8), ("tma_x2", 9), ("tb2_64x16", 11), ("tb2_64x8", 12), ("vec", 10)):
+        for dname, x, y, dt in (("fp32", a, b, 0), ("fp16", ha, hb, 3)):
+            tiles["%s_%s_ms" % (tname, dname)] = steps_only(x, y, dt, tid)
+    res["step_ms_by_tile"] = tiles
+    for label, x, y, x0, dt, bpl in (("chosen_fp32", a, b, f32, 0, 8), ("chosen_fp16_storage", ha, hb, h0, 3, 4)):
+        tile, kz, tms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_float(0)
+        x.copy_(x0)
+        gb.call("appfis_gb_star_r4_tune", x.data_ptr(), y.data_ptr(), dt, nx, ny, nz, nx + 8, 1, 0.0, w, ctypes.byref(tile),
+                ctypes.byref(kz), ctypes.byref(tms), sp.cuda_stream)
+        ms = _time(torch, sp, run(x, y, x0, dt, it, AUTO))  # AUTO runs the tuned choice
+        err = _err((x if ci.value == 0 else y).float(), r64)
+        sm = steps_only(x, y, dt, AUTO)
+        gbs = nx * ny * nz * bpl / (sm * 1e-3) / 1e9
+        res[label] = {"glups": lups / (ms * 1e-3) / 1e9, "ms": ms, "speedup_vs_plain": ms32 / ms, "sweep_ms": sm,
+                      "tuned": {"tile": tile.value, "kernel": names.get(tile.value, str(tile.value)),
+                                "steps_per_launch": 2 if tile.value in (11, 12) else 1,
+                                "zchunk": kz.value, "tuner_ms_per_step": tms.value},
+                      "bytes_per_lup": bpl, "achieved_gbs": gbs, "frac_of_hbm": gbs / hbm, "error_vs_fp64": err}
+    del x64, y64, r64
     return res
 
 
@@ -913,12 +925,16 @@ def profile_small(name, torch, gb, W, dev, sp):
         w = (ctypes.c_float * 5)(*W.fdtd_weights())
         f = torch.from_numpy(W.fdtd_padded(nx, ny, nz, c["seed"])).to(dev)
         a, b = f.clone(), f.clone()
-        gb.call("appfis_gb_star_r4", a.data_ptr(), b.data_ptr(), 0, nx, ny, nz, nx + 8, 5, 1, 0.0, w, 0, 0, ctypes.byref(ci),
+        gb.call("appfis_gb_star_r4", a.data_ptr(), b.data_ptr(), 0, nx, ny, nz, nx + 8, 5, 1, 0.0, w, 8, 0, ctypes.byref(ci),
                 sp.cuda_stream)
         h = f.half()
         ha, hb = h.clone(), h.clone()
-        gb.call("appfis_gb_star_r4", ha.data_ptr(), hb.data_ptr(), 3, nx, ny, nz, nx + 8, 5, 1, 0.0, w, 0, 0, ctypes.byref(ci),
+        gb.call("appfis_gb_star_r4", ha.data_ptr(), hb.data_ptr(), 3, nx, ny, nz, nx + 8, 5, 1, 0.0, w, 8, 0, ctypes.byref(ci),
                 sp.cuda_stream)
+        # the two-step time-blocked tile: 2 launches (4 steps) in FP32, then in FP16 storage
+        for x, y, dt in ((a, b, 0), (ha, hb, 3)):
+            gb.call("appfis_gb_star_r4", x.data_ptr(), y.data_ptr(), dt, nx, ny, nz, nx + 8, 4, 1, 0.0, w, 11, 0,
+                    ctypes.byref(ci), sp.cuda_stream)
 
 
 def profile_case(name, local):
@@ -927,7 +943,8 @@ def profile_case(name, local):
             life_bits_sweep) then 20 u8 sweeps (life_u8_bulk)
     himeno: 257x257x513 (rows padded to 264), 5 plain sweeps (himeno_tma<0>), 5 mixed sweeps
             (himeno_tma<1>, himeno_correct)
-    fdtd:   512^3, 5 FP32 steps then 5 FP16 steps (star_r4_tma)
+    fdtd:   512^3, 5 FP32 steps then 5 FP16 steps (star_r4_tma), then 2 two-step launches in FP32
+            and 2 in FP16 (star_r4_tb2)
     heat:   1024^2, 16 iterations (2 heat2d_regs launches)
     flood:  the 32-domain batch (80 M cells, ~2.6 GB), 20 steps (one flood_persistent launch)"""
     import torch

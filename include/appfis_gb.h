@@ -215,6 +215,9 @@ APPFIS_GB_API int appfis_gb_himeno_job(const float* coef_host, float* p_host, in
 #define APPFIS_GB_STAR_TMA_X4 8  /* TMA-staged 64 x 16 tile, 4 x points x 2 rows per thread */
 #define APPFIS_GB_STAR_TMA_X2 9  /* TMA-staged 32 x 16 tile, 2 x points x 2 rows per thread */
 #define APPFIS_GB_STAR_VEC 10    /* register-staged 64 x 16 tile of 4-element vectors */
+#define APPFIS_GB_STAR_TB2 11    /* TMA-staged, TWO time steps per launch (64 x 16 output tile, step-1 values kept on
+                                    chip); an odd last step runs in the TMA_X4 tile */
+#define APPFIS_GB_STAR_TB2_8 12  /* the same with a 64 x 8 output tile */
 /* Replaces the per-step Execute3D(config, coeff, radius, cur, next) of the FDTD3d functor
  * (FDTD3d/src/fdtd3d_appfis.hpp:84-87,129-143) with radius 4 on a DUAL grid with a ghost halo of
  * width 4 (a, b: padded (nx+8) x (ny+8) x (nz+8), pitch >= nx+8, halo held at its values).
@@ -222,8 +225,9 @@ APPFIS_GB_API int appfis_gb_himeno_job(const float* coef_host, float* p_host, in
  *         v *= coeff  (same order; FP32 results bit-identical to the reference CPU path).
  * mode 1: weighted form  v = w[0]*c + sum_a w[a]*((x-a + x+a) + (y-a + y+a) + (z-a + z+a)).
  * dtype: APPFIS_GB_F32 or APPFIS_GB_F16 (storage).  tile selects the kernel (APPFIS_GB_STAR_*;
- * AUTO: the TMA-staged tile when rows and fields are 16-byte aligned, else the vector tile when
- * 4-element vectors are aligned, else the scalar tile; all give the same results).  zchunk: z
+ * AUTO: the choice appfis_gb_star_r4_tune recorded for this device and shape, else the TMA-staged
+ * tile when rows and fields are 16-byte aligned, else the vector tile when 4-element vectors are
+ * aligned, else the scalar tile; all give the same results in the reference form and in FP32).  zchunk: z
  * planes per CTA (0 = the tile's default: TMA-staged 32-64 planes balanced over nz, the length that fills the
  * resident CTAs in the most nearly whole waves; 32 otherwise). */
 APPFIS_GB_API int appfis_gb_star_r4(void* a, void* b, int dtype, int nx, int ny, int nz, int pitch, int iters, int mode,
@@ -248,6 +252,19 @@ APPFIS_GB_API int appfis_gb_himeno_f64(const double* const* coef, double* p, dou
  * (mode 1, 5 double weights) in double, halo width 4. */
 APPFIS_GB_API int appfis_gb_star_r4_f64(double* a, double* b, int nx, int ny, int nz, int pitch, int iters, int mode,
                                         double coeff, const double* weights, int* cur_index, void* stream);
+
+/* Autotuner of the radius-4 star (no counterpart in the reference): times every candidate kernel
+ * for this shape on `stream` — on 16-byte rows the TMA-staged tiles (4 or 2 x points per thread,
+ * one step per launch) and the two-step time-blocked tiles (64 x 16 / 64 x 8 outputs), else the
+ * vector / scalar tiles — with z chunks of the tile's default and 32 .. 256 planes, each run
+ * from a into b (b's interior is overwritten; a and the halos are not), and keeps the fastest
+ * per device and shape (dtype, form, nx, ny, nz, pitch) for the process; later calls with
+ * tile = APPFIS_GB_STAR_AUTO use it (zchunk 0 = the tuned chunk).  With APPFIS_GB_TUNE_FILE set
+ * in the environment, results are read from / appended to that text file.  Returns the choice
+ * (tile id, z chunk; 0 = the tile's default) and its time per step; synchronises `stream`. */
+APPFIS_GB_API int appfis_gb_star_r4_tune(void* a, void* b, int dtype, int nx, int ny, int nz, int pitch, int mode, float coeff,
+                                         const float* weights, int* tile_out, int* zchunk_out, float* ms_per_step_out,
+                                         void* stream);
 
 /* ----------------------------------------------------------------------------- Triton flood model */
 /* Replaces the reference's Triton time loop (Triton/src/triton_appfis.hpp:316-386: CFL dt functor +

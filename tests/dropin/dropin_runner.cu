@@ -11,6 +11,9 @@
 //        dropin_runner fdtd   NX NY NZ ITERS COEFF in.f32 out.f32
 //        dropin_runner triton NX NY DX CN HEXTRA MANN T_END PRINT TSTEP MAXSTEPS dem.f64 h.f64 out.f64 dt.f64
 //        dropin_runner ireduce NX NY in.i32           (Execute2DReduce SUM / MAX / MIN of an int grid)
+//        dropin_runner star_periodic NX NY NZ ITERS in.f32 plain.f32 overlap.f32
+//                      the radius-4 star on a PERIODIC grid, once with Execute3D and once with
+//                      ExecuteOverlap3D (boundary slabs, then the ghost refresh behind the interior)
 //        dropin_runner ckpt NX NY G1 G2 in.u8 a.u8 b.u8 DIR [fast]
 //                      GameOfLife: G1 generations, SaveDeviceState, G2 more -> a; a second grid
 //                      restored with LoadDeviceState, G2 generations -> b (a == b == G1 + G2
@@ -462,6 +465,39 @@ static std::vector<unsigned char> GolInterior(APPFIS::Grid<int>& g, int nx, int 
 	return out;
 }
 
+static int RunStarPeriodic(int argc, char** argv)
+{
+	const int nx = std::atoi(argv[2]), ny = std::atoi(argv[3]), nz = std::atoi(argv[4]), iters = std::atoi(argv[5]);
+	std::vector<char> in = ReadFile(argv[6], (size_t)nx * ny * nz * sizeof(float));
+	const int radius = 4;
+	const float coeff = 0.05f;
+	APPFIS::Attribute attr;
+	attr.ghostLayer = radius;
+	attr.periodic = true;
+	APPFIS::Initialize(argc, argv, APPFIS::DIM_3D, APPFIS::DIM_3D, attr);
+	for (int form = 0; form < 2; form++)
+	{
+		APPFIS::Grid<float> g(APPFIS::DIM_3D, nx, ny, nz, APPFIS::DUAL);
+		g.AllocateFullGrid();
+		std::memcpy(g.GetFullGrid()->GetData(), in.data(), in.size());
+		APPFIS::Scatter(g.GetFullGrid(), g.GetSubGrid());
+		APPFIS::Config<float> config(g);
+		config.GridsToUpdate(g);
+		APPFIS::InitializeExecution(g);
+		for (int t = 0; t < iters; t++)
+		{
+			if (form == 0) APPFIS::Execute3D(config, coeff, radius, g.GetSubGrid(), g.GetSubGridNext());
+			else APPFIS::ExecuteOverlap3D(config, coeff, radius, g.GetSubGrid(), g.GetSubGridNext());
+		}
+		APPFIS::FinalizeExecution(g);
+		APPFIS::Array<float>* sub = g.GetSubGrid();
+		WriteFile(argv[7 + form], sub->GetData(), sizeof(float) * (size_t)sub->GetSize());
+	}
+	std::printf("{\"ok\": true}\n");
+	APPFIS::Finalize();
+	return 0;
+}
+
 // Checkpoint / restart through the device state, and the host binary-file round trip.
 static int RunCheckpoint(int argc, char** argv)
 {
@@ -517,6 +553,7 @@ int main(int argc, char** argv)
 	if (mode == "triton") return RunTriton(argc, argv);
 	if (mode == "ireduce") return RunIntReduce(argc, argv);
 	if (mode == "ckpt") return RunCheckpoint(argc, argv);
+	if (mode == "star_periodic") return RunStarPeriodic(argc, argv);
 	std::fprintf(stderr, "unknown mode %s\n", argv[1]);
 	return 2;
 }

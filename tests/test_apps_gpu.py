@@ -61,6 +61,8 @@ def values(out, keys):
     ("HeatDiffusion", ["-dimx=33", "-dimy=17", "-dimz=9", "-iteration=7"], ["Max", "Min"], 0),
     ("GameOfLife", ["-dimx=300", "-dimy=200", "-iteration=50"], ["Live Count"], 0),
     ("GameOfLife", ["-dimx=67", "-dimy=45", "-iteration=31"], ["Live Count"], 0),
+    # -overlap: the overlapped executors on both sides (strips first, the ghost refresh behind the interior)
+    ("GameOfLife", ["-dimx=300", "-dimy=200", "-iteration=50", "-overlap"], ["Live Count"], 0),
     ("Himeno", ["-dimx=65", "-dimy=65", "-dimz=129", "-iteration=20"], ["Sum"], 2e-4),
     ("Himeno", ["-dimx=33", "-dimy=17", "-dimz=20", "-iteration=5"], ["Sum"], 2e-4),
 ])

@@ -119,3 +119,61 @@ def test_fp16_tma_and_vector_tiles_agree(gb, torch_cuda):
     a = run(gb, torch_cuda, f, 4, 1, weights=w, dtype="f16", pitch=72)
     b = run(gb, torch_cuda, f, 4, 1, weights=w, dtype="f16", pitch=76)
     assert np.abs(a - b).max() <= 1e-3
+
+
+TB2, TB2_8 = 11, 12  # time-blocked tiles: two steps per launch (64 x 16 / 64 x 8 output tiles)
+
+
+@pytest.mark.parametrize("tile", [TB2, TB2_8])
+@pytest.mark.parametrize("nx,ny,nz,iters,kz,pitch", [(64, 70, 33, 2, 16, 72), (37, 29, 11, 3, 0, 48), (130, 17, 21, 4, 8, 140),
+                                                     (9, 16, 1, 2, 0, 20), (64, 16, 40, 6, 0, 72), (4, 1, 2, 5, 0, 12),
+                                                     (200, 45, 70, 4, 24, 208)])
+def test_time_blocked_reference_form_vs_oracle(gb, torch_cuda, tile, nx, ny, nz, iters, kz, pitch):
+    """Two steps per launch (an odd last step in the single-step tile): bit-identical to the
+    oracle's step-by-step run of the reference form — aligned and ragged x / y / z, short z
+    chunks, a single plane, odd and even step counts."""
+    f = W.fdtd_padded(nx, ny, nz, 5 * nx + nz)
+    out = run(gb, torch_cuda, f, iters, 0, 0.1, pitch=pitch, ry=tile, kz=kz)
+    assert np.array_equal(out, O.star_r4(f, iters, coeff=0.1))
+
+
+@pytest.mark.parametrize("tile", [TB2, TB2_8])
+def test_time_blocked_weighted_equals_single_step(gb, torch_cuda, tile):
+    """The weighted form in FP32: the time-blocked tile does the single-step tile's arithmetic in
+    the same order, so 6 steps agree bit for bit."""
+    w = W.fdtd_weights()
+    f = W.fdtd_padded(96, 40, 30, 23)
+    a = run(gb, torch_cuda, f, 6, 1, weights=w, pitch=104, ry=tile)
+    b = run(gb, torch_cuda, f, 6, 1, weights=w, pitch=104, ry=TMA_X4)
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("tile", [TB2, TB2_8])
+def test_time_blocked_fp16_error(gb, torch_cuda, tile):
+    """FP16 storage with the step-1 values kept in FP32 on chip: within the FP16 form's 2e-3 of
+    the FP64 oracle after 50 steps."""
+    w = W.fdtd_weights()
+    f = W.fdtd_padded(64, 64, 64, 9)
+    ref64 = O.star_r4(f.astype(np.float64), 50, weights=w, dtype=np.float64)
+    o16 = run(gb, torch_cuda, f, 50, 1, weights=w, dtype="f16", ry=tile)
+    assert np.abs(o16 - ref64).max() < 2e-3
+
+
+def test_autotuner_choice_is_used_and_exact(gb, torch_cuda):
+    """appfis_gb_star_r4_tune times the candidates from a into b (a and the halo untouched),
+    returns a tile of the aligned-row set, and AUTO then runs that choice: the reference form
+    stays bit-identical to the oracle."""
+    torch = torch_cuda
+    nx, ny, nz, pitch = 96, 40, 70, 104
+    f = W.fdtd_padded(nx, ny, nz, 77)
+    host = np.zeros(f.shape[:2] + (pitch,), dtype=np.float32)
+    host[..., : nx + 8] = f
+    a = torch.from_numpy(host).cuda()
+    b = a.clone()
+    tile, kz, ms = ctypes.c_int(-1), ctypes.c_int(-1), ctypes.c_float(-1)
+    gb.call("appfis_gb_star_r4_tune", a.data_ptr(), b.data_ptr(), 0, nx, ny, nz, pitch, 0, 0.1, None, ctypes.byref(tile),
+            ctypes.byref(kz), ctypes.byref(ms), None)
+    assert tile.value in (TMA_X4, TMA_X2, TB2, TB2_8) and kz.value >= 0 and ms.value > 0
+    assert torch.equal(a, torch.from_numpy(host).cuda())  # the input was not written
+    out = run(gb, torch_cuda, f, 5, 0, 0.1, pitch=pitch, ry=0)
+    assert np.array_equal(out, O.star_r4(f, 5, coeff=0.1))
