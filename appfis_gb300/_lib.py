@@ -16,7 +16,7 @@ F32, F64, I32, F16 = 0, 1, 2, 3
 MAX, MIN, SUM = 0, 1, 2
 LIFE_REFERENCE, LIFE_B3S23 = 0, 1
 FORM_U8, FORM_BITS = 0, 1
-STAR_AUTO, STAR_SCALAR2, STAR_SCALAR4, STAR_TMA_X4, STAR_TMA_X2, STAR_VEC, STAR_TB2, STAR_TB2_8 = 0, 2, 4, 8, 9, 10, 11, 12
+STAR_AUTO, STAR_SCALAR2, STAR_SCALAR4, STAR_TMA_X4, STAR_TMA_X2, STAR_VEC, STAR_TB2, STAR_TB2_8, STAR_TMA_X4R4 = 0, 2, 4, 8, 9, 10, 11, 12, 13
 
 _P = ctypes.c_void_p
 _i = ctypes.c_int

@@ -438,23 +438,37 @@ constexpr int MCT = 10 * MX * MY * 2 + MX * MY * 4 + MX * MY * 2;  // per-point 
 constexpr int MSTG = MCT + MES;                         // one stage
 constexpr int MR32 = MW * (MY + 2);                     // floats per FP32 ring slot
 constexpr int MIX_S = 2;
-constexpr int mixed2_smem(int S) { return S * MSTG + 4 * MR32 * 4 + 3 * MES + S * 8; }
 
+// The tile of width TW and its byte sizes.
+template <int TW>
+struct MixTile {
+    static constexpr int X = TW, W = TW + 2 * MXO;
+    static constexpr int EB = W * (MY + 2) * 2, ES = (EB + 127) / 128 * 128;
+    static constexpr int CT = 10 * X * MY * 2 + X * MY * 4 + X * MY * 2;
+    static constexpr int STG = CT + ES, R32 = W * (MY + 2);
+    static constexpr int smem(int S) { return S * STG + 4 * R32 * 4 + 3 * ES + S * 8; }
+};
+
+template <int TW>
 __device__ __forceinline__ void e_box_to_f32(const unsigned char* src, float* dst, int t)
 {
     const __half2* h = reinterpret_cast<const __half2*>(src);
     float2* d = reinterpret_cast<float2*>(dst);
-    for (int q = t; q < MR32 / 2; q += MX / 2 * MY) d[q] = __half22float2(h[q]);
+    for (int q = t; q < MixTile<TW>::R32 / 2; q += TW / 2 * MY) d[q] = __half22float2(h[q]);
 }
 
-template <int S>
-__global__ void __launch_bounds__(MX / 2 * MY) himeno_mixed2(const __grid_constant__ TileMaps maps, __half* __restrict__ eout,
+// TW: tile width in x points (64 or 72: the launcher takes the one whose whole tiles cover the
+// grid's columns with less overhang).
+template <int S, int TW>
+__global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_constant__ TileMaps maps, __half* __restrict__ eout,
                                                              int nx, int ny, int nz, int pitch, int py, int kz, float omega,
                                                              float inv_omega, double* __restrict__ partials,
                                                              unsigned* __restrict__ ticket, double* __restrict__ gosa,
                                                              unsigned* __restrict__ status)
 {
     namespace f2 = gb::f2;
+    typedef MixTile<TW> L;
+    constexpr int MX = L::X, MW = L::W, MEB = L::EB, MES = L::ES, MCT = L::CT, MSTG = L::STG, MR32 = L::R32;
     extern __shared__ __align__(128) unsigned char tsm[];
     unsigned char* stages = tsm;
     float* ring = reinterpret_cast<float*>(tsm + S * MSTG);
@@ -504,10 +518,10 @@ __global__ void __launch_bounds__(MX / 2 * MY) himeno_mixed2(const __grid_consta
         if (!gb::tma::wait(&bar[s], (unsigned)((k - k0) / S) & 1u)) bad = true;
         const unsigned char* st = stages + s * MSTG;
         if (k == k0) {  // uniform
-            for (int d = 0; d < 3; d++) e_box_to_f32(pro + d * MES, slot(k0 - 1 + d), t);
+            for (int d = 0; d < 3; d++) e_box_to_f32<TW>(pro + d * MES, slot(k0 - 1 + d), t);
             __syncthreads();
         }
-        e_box_to_f32(st + MCT, slot(k + 2), t);  // plane k+2 into the slot plane k-2 left
+        e_box_to_f32<TW>(st + MCT, slot(k + 2), t);  // plane k+2 into the slot plane k-2 left
         {
             const float* sm = slot(k - 1);
             const float* s0 = slot(k);
@@ -573,8 +587,7 @@ __global__ void __launch_bounds__(MX / 2 * MY) himeno_mixed2(const __grid_consta
         for (int kk = k; kk < min(k + S, k1); kk++)
                 gb::tma::wait(&bar[(kk - k0) % S], (unsigned)((kk - k0) / S) & 1u, gb::tma::DRAIN_NS);
     }
-    if (gosa)
-        gosa_reduce(k < k1 ? __longlong_as_double(0x7ff8000000000000ll) : (double)g.x + (double)g.y, partials, ticket, gosa);
+    if (gosa) gosa_reduce(k < k1 ? __longlong_as_double(0x7ff8000000000000ll) : (double)g.x + (double)g.y, partials, ticket, gosa);
 }
 
 // ---------------------------------------------------------------- TMA-staged correction pass
@@ -815,28 +828,35 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     // TMA-staged inner sweeps (two points per thread) when the FP16 rows are 16-byte aligned
     // (pitch a multiple of 8)
     const bool use_tma = pitch % 8 == 0 && gb::aligned16(hw) && gb::aligned16(coef[3]);
-    constexpr int tsmem = mixed2_smem(MIX_S);
+    // A tile costs the same per plane however few of its columns lie inside the grid, so the
+    // inner sweep takes the tile width whose whole tiles overhang columns 0 .. nx+1 less: 257
+    // interior columns take four 72-wide tiles (288 columns) rather than five 64-wide ones (320).
+    const int tiles64 = gb::ceil_div(nx + 1, 64), tiles72 = gb::ceil_div(nx + 1, 72);
+    const int tw = tiles72 * 72 < tiles64 * 64 ? 72 : 64;
+    const int tiles_x = tw == 72 ? tiles72 : tiles64;
+    const int tsmem = tw == 72 ? MixTile<72>::smem(MIX_S) : MixTile<64>::smem(MIX_S);
+    const int tbox_e = tw == 72 ? MixTile<72>::W : MixTile<64>::W;
+    auto tkern = tw == 72 ? himeno_mixed2<MIX_S, 72> : himeno_mixed2<MIX_S, 64>;
     int tkz = gb::balanced_chunk(nz, HKZ);
     if (use_tma) {  // z chunks that fill the resident CTAs in whole waves (only e re-reads a halo)
-        GB_CUDA(cudaFuncSetAttribute(himeno_mixed2<MIX_S>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem));
+        GB_CUDA(cudaFuncSetAttribute(tkern, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem));
         int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, himeno_mixed2<MIX_S>, MX / 2 * MY, tsmem) != cudaSuccess ||
-            per_sm < 1)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tkern, tw / 2 * MY, tsmem) != cudaSuccess || per_sm < 1)
             per_sm = 1;
-        tkz = gb::wave_chunk(nz, 32, 64, (long long)(nx / MX + 1) * gb::ceil_div(ny, MY), (long long)per_sm * gb::sm_count(), 0);
+        tkz = gb::wave_chunk(nz, 32, 64, (long long)tiles_x * gb::ceil_div(ny, MY), (long long)per_sm * gb::sm_count(), 0);
     }
-    dim3 tblk(MX / 2, MY), tgrd(nx / MX + 1, gb::ceil_div(ny, MY), gb::ceil_div(nz, tkz));
+    dim3 tblk(tw / 2, MY), tgrd(tiles_x, gb::ceil_div(ny, MY), gb::ceil_div(nz, tkz));
     TileMaps tmaps[2];
     unsigned* status = nullptr;
     if (use_tma) {
         const int py = ny + 2;
         for (int n = 0; n < 10; n++)
-            GB_TRY(gb::tensor_map_3d(&tmaps[0].m[n], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, hf.c[n], nx + 2, py, nz + 2, pitch, py, MX, MY));
-        GB_TRY(gb::tensor_map_3d(&tmaps[0].m[10], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, coef[3], nx + 2, py, nz + 2, pitch, py, MX, MY));
-        GB_TRY(gb::tensor_map_3d(&tmaps[0].m[11], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, Dd, nx + 2, py, nz + 2, pitch, py, MX, MY));
+            GB_TRY(gb::tensor_map_3d(&tmaps[0].m[n], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, hf.c[n], nx + 2, py, nz + 2, pitch, py, tw, MY));
+        GB_TRY(gb::tensor_map_3d(&tmaps[0].m[10], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, coef[3], nx + 2, py, nz + 2, pitch, py, tw, MY));
+        GB_TRY(gb::tensor_map_3d(&tmaps[0].m[11], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, Dd, nx + 2, py, nz + 2, pitch, py, tw, MY));
         tmaps[1] = tmaps[0];
         for (int b = 0; b < 2; b++)
-            GB_TRY(gb::tensor_map_3d(&tmaps[b].m[12], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, E[b], nx + 2, py, nz + 2, pitch, py, MW,
+            GB_TRY(gb::tensor_map_3d(&tmaps[b].m[12], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, E[b], nx + 2, py, nz + 2, pitch, py, tbox_e,
                                      MY + 2));
         GB_TRY(gb::status_word(&status));
     }
@@ -877,10 +897,10 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     correct();  // D from the initial P (e = 0), e restarted at 0
     const float inv_omega = 1.0f / omega;
     for (int it = 0; it < iters; it++) {
-        if (use_tma)
-            himeno_mixed2<MIX_S><<<tgrd, tblk, tsmem, st>>>(tmaps[ec], E[1 - ec], nx, ny, nz, pitch, ny + 2, tkz, omega, inv_omega,
-                                                           rpartials, rticket, dev_gosa ? dev_gosa + it : nullptr, status);
-        else
+        if (use_tma) {
+            tkern<<<tgrd, tblk, tsmem, st>>>(tmaps[ec], E[1 - ec], nx, ny, nz, pitch, ny + 2, tkz, omega, inv_omega, rpartials, rticket,
+                                             dev_gosa ? dev_gosa + it : nullptr, status);
+        } else
             himeno_ring<1><<<rgrd, rblk, 0, st>>>(cf, hf, E[ec], E[1 - ec], Dd, nx, ny, nz, pitch, ny + 2, HKZ, omega, inv_omega,
                                                   rpartials, rticket, dev_gosa ? dev_gosa + it : nullptr);
         ec = 1 - ec;

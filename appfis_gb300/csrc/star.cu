@@ -327,11 +327,13 @@ __global__ void __launch_bounds__(256) star_r4_vec(const T* __restrict__ in, T* 
 // (twice the resident warps).  Global traffic: each plane read once per CTA (plus the 8-plane
 // z-chunk overlap), each result written once.
 constexpr int TNS = 8;   // ring slots: planes k..k+4 resident, 3 more in flight
-constexpr int TRY = 2;   // rows per thread
-constexpr int TTY = 16;  // tile rows (8 thread rows x TRY)
 
-template <class T, int VXT>
+// TRY rows per thread (2, or 4 for the tile that spreads each plane's fixed per-thread work --
+// the mbarrier wait, the ring addresses, the barrier, the store predicates -- over 16 points);
+// the tile has 8 thread rows, TTY = 8 * TRY rows.
+template <class T, int VXT, int TRY = 2>
 struct TmaStar {
+    static constexpr int TTY = 8 * TRY;             // tile rows
     static constexpr int TX = 16 * VXT;             // tile x points
     static constexpr int SW = TX + 2 * R, SH = TTY + 2 * R;
     static constexpr int BOX = SW * SH * (int)sizeof(T);  // bytes per plane box
@@ -388,15 +390,15 @@ template <> __device__ __forceinline__ void stgv<__half, 2>(__half* p, const flo
 // Waits: `wait_ns` per mbarrier wait (1 s in production); `shortfall` (testing only, 0 in
 // production) arms the first plane's barrier with that many bytes more than its copy delivers,
 // so that its wait runs out.
-template <class T, int MODE, int VXT>
-__global__ void __launch_bounds__(128, VXT == 4 ? 4 : 6) star_r4_tma(const __grid_constant__ CUtensorMap map, T* __restrict__ out,
+template <class T, int MODE, int VXT, int TRY>
+__global__ void __launch_bounds__(128, VXT == 4 ? (TRY == 2 ? 4 : 2) : 6) star_r4_tma(const __grid_constant__ CUtensorMap map, T* __restrict__ out,
                                                                      int nx, int ny, int nz, int px, int py, int kz, float coeff,
                                                                      StarW wt, unsigned* __restrict__ status,
                                                                      unsigned long long wait_ns, unsigned shortfall)
 {
     namespace f2 = gb::f2;
-    typedef TmaStar<T, VXT> Lay;
-    constexpr int SW = Lay::SW;
+    typedef TmaStar<T, VXT, TRY> Lay;
+    constexpr int SW = Lay::SW, TTY = Lay::TTY;
     extern __shared__ __align__(128) unsigned char tsm[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(tsm + TNS * Lay::SLOT);
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * 16 + tx;
@@ -416,16 +418,17 @@ __global__ void __launch_bounds__(128, VXT == 4 ? 4 : 6) star_r4_tma(const __gri
     }
     __syncthreads();
     const int pbase = k0 - R;  // plane of slot 0, phase 0
-    auto slot = [&](int pl) { return reinterpret_cast<const T*>(tsm + ((pl - pbase) % TNS) * Lay::SLOT); };
+    // plane offsets from pbase are never negative: unsigned arithmetic makes the ring index a mask
+    auto slot = [&](int pl) { return reinterpret_cast<const T*>(tsm + ((unsigned)(pl - pbase) % TNS) * Lay::SLOT); };
     int last_issued = pbase - 1;  // thread 0 only
     auto issue = [&](int pl) {
         last_issued = pl;
-        const int n = (pl - pbase) % TNS;
+        const unsigned n = (unsigned)(pl - pbase) % TNS;
         gb::tma::arrive_expect(&bar[n], Lay::BOX + (pl == pbase ? shortfall : 0u));
         gb::tma::load_3d(tsm + n * Lay::SLOT, &map, bx0, by0, pl, &bar[n]);
     };
     auto ready = [&](int pl, uint64_t limit) {
-        return gb::tma::wait(&bar[(pl - pbase) % TNS], (unsigned)((pl - pbase) / TNS) & 1u, limit);
+        return gb::tma::wait(&bar[(unsigned)(pl - pbase) % TNS], ((unsigned)(pl - pbase) / TNS) & 1u, limit);
     };
     if (t == 0)
         for (int pl = pbase; pl < pbase + TNS && pl <= plast; pl++) issue(pl);
@@ -641,17 +644,17 @@ __global__ void __launch_bounds__(TbStar<T, TY>::NT, 1) star_r4_tb2(const __grid
         gb::tma::prefetch_map(&map);
     }
     __syncthreads();
-    auto slot = [&](int pl) { return reinterpret_cast<const T*>(tsm + ((pl - pbase) % TB_NS) * Lay::SLOT); };
-    auto l1slot = [&](int q) { return l1 + (size_t)((q - pbase) % TB_L1) * (Lay::L1S / 4); };
+    auto slot = [&](int pl) { return reinterpret_cast<const T*>(tsm + ((unsigned)(pl - pbase) % TB_NS) * Lay::SLOT); };
+    auto l1slot = [&](int q) { return l1 + (size_t)((unsigned)(q - pbase) % TB_L1) * (Lay::L1S / 4); };
     int last_issued = pbase - 1;
     auto issue = [&](int pl) {
         last_issued = pl;
-        const int n = (pl - pbase) % TB_NS;
+        const unsigned n = (unsigned)(pl - pbase) % TB_NS;
         gb::tma::arrive_expect(&bar[n], Lay::BOX);
         gb::tma::load_3d(tsm + n * Lay::SLOT, &map, bx0, by0, pl, &bar[n]);
     };
     auto ready = [&](int pl, uint64_t limit) {
-        return gb::tma::wait(&bar[(pl - pbase) % TB_NS], (unsigned)((pl - pbase) / TB_NS) & 1u, limit);
+        return gb::tma::wait(&bar[(unsigned)(pl - pbase) % TB_NS], ((unsigned)(pl - pbase) / TB_NS) & 1u, limit);
     };
     if (t == 0)
         for (int pl = pbase; pl < pbase + TB_NS && pl <= plast; pl++) issue(pl);
@@ -782,11 +785,12 @@ void launch_star(const T* in, T* out, int nx, int ny, int nz, int px, int kz, fl
     star_r4_sweep<T, MODE, RY><<<grd, blk, 0, st>>>(in, out, nx, ny, nz, px, ny + 2 * R, kz, coeff, w);
 }
 
-template <class T, int VXT>
+template <class T, int VXT, int TRY = 2>
 int run_star_tma(T** buf, int nx, int ny, int nz, int pitch, int iters, int mode, float coeff, StarW w, int kz, int* cur_index,
                  cudaStream_t st)
 {
-    typedef TmaStar<T, VXT> Lay;
+    typedef TmaStar<T, VXT, TRY> Lay;
+    constexpr int TTY = Lay::TTY;
     const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
     CUtensorMap maps[2];
     for (int n = 0; n < 2; n++)
@@ -795,7 +799,7 @@ int run_star_tma(T** buf, int nx, int ny, int nz, int pitch, int iters, int mode
     unsigned* status;
     GB_TRY(gb::status_word(&status));
     constexpr int smem = Lay::smem();
-    auto kern = mode == 0 ? star_r4_tma<T, 0, VXT> : star_r4_tma<T, 1, VXT>;
+    auto kern = mode == 0 ? star_r4_tma<T, 0, VXT, TRY> : star_r4_tma<T, 1, VXT, TRY>;
     GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     // default z chunk: 32-64 planes per CTA, the length whose grid fills the resident CTAs in the
     // most nearly whole waves, counting the 8 halo planes each chunk re-reads (512^3: 47 planes,
@@ -928,7 +932,8 @@ int tune_star(T* a, T* b, int dtype, int nx, int ny, int nz, int pitch, int mode
     const bool rows16 = (pitch * sizeof(T)) % 16 == 0 && gb::aligned16(a) && gb::aligned16(b);
     const bool vec4 = pitch % 4 == 0 && ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) % (sizeof(T) * 4)) == 0;
     std::vector<int> tiles;
-    if (rows16) tiles = {APPFIS_GB_STAR_TMA_X4, APPFIS_GB_STAR_TMA_X2, APPFIS_GB_STAR_TB2, APPFIS_GB_STAR_TB2_8};
+    if (rows16)
+        tiles = {APPFIS_GB_STAR_TMA_X4, APPFIS_GB_STAR_TMA_X4R4, APPFIS_GB_STAR_TMA_X2, APPFIS_GB_STAR_TB2, APPFIS_GB_STAR_TB2_8};
     else if (vec4) tiles = {APPFIS_GB_STAR_VEC, APPFIS_GB_STAR_SCALAR4};
     else tiles = {APPFIS_GB_STAR_SCALAR4, APPFIS_GB_STAR_SCALAR2};
     std::vector<int> chunks = {0};
@@ -981,7 +986,8 @@ int run_star(T* a, T* b, int nx, int ny, int nz, int pitch, int iters, int mode,
     const bool vec4 = pitch % 4 == 0 && ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) % (sizeof(T) * 4)) == 0;
     if (tile == APPFIS_GB_STAR_AUTO)  // TMA-staged when rows are 16-byte aligned, else vectors, else scalar
         tile = rows16 ? APPFIS_GB_STAR_TMA_X4 : (vec4 ? APPFIS_GB_STAR_VEC : APPFIS_GB_STAR_SCALAR4);
-    if ((tile == APPFIS_GB_STAR_TMA_X4 || tile == APPFIS_GB_STAR_TMA_X2 || tile == APPFIS_GB_STAR_TB2 || tile == APPFIS_GB_STAR_TB2_8) &&
+    if ((tile == APPFIS_GB_STAR_TMA_X4 || tile == APPFIS_GB_STAR_TMA_X2 || tile == APPFIS_GB_STAR_TB2 || tile == APPFIS_GB_STAR_TB2_8 ||
+         tile == APPFIS_GB_STAR_TMA_X4R4) &&
         !rows16)
         return gb::fail(APPFIS_GB_EINVAL, "star_r4: the TMA-staged tiles need 16-byte aligned rows and fields");
     if (tile == APPFIS_GB_STAR_VEC && !vec4)
@@ -1003,6 +1009,8 @@ int run_star(T* a, T* b, int nx, int ny, int nz, int pitch, int iters, int mode,
         return APPFIS_GB_OK;
     }
     if (tile == APPFIS_GB_STAR_TMA_X4) return run_star_tma<T, 4>(buf, nx, ny, nz, pitch, iters, mode, coeff, w, kz, cur_index, st);
+    if (tile == APPFIS_GB_STAR_TMA_X4R4)
+        return run_star_tma<T, 4, 4>(buf, nx, ny, nz, pitch, iters, mode, coeff, w, kz, cur_index, st);
     if (tile == APPFIS_GB_STAR_TMA_X2) return run_star_tma<T, 2>(buf, nx, ny, nz, pitch, iters, mode, coeff, w, kz, cur_index, st);
     if (kz <= 0) kz = 32;
     int ci = 0;
@@ -1039,7 +1047,7 @@ int appfis_gb_star_r4(void* a, void* b, int dtype, int nx, int ny, int nz, int p
     if (iters < 0) return gb::fail(APPFIS_GB_EINVAL, "star_r4: negative iteration count");
     if (tile != APPFIS_GB_STAR_AUTO && tile != APPFIS_GB_STAR_SCALAR2 && tile != APPFIS_GB_STAR_SCALAR4 &&
         tile != APPFIS_GB_STAR_TMA_X4 && tile != APPFIS_GB_STAR_TMA_X2 && tile != APPFIS_GB_STAR_VEC && tile != APPFIS_GB_STAR_TB2 &&
-        tile != APPFIS_GB_STAR_TB2_8)
+        tile != APPFIS_GB_STAR_TB2_8 && tile != APPFIS_GB_STAR_TMA_X4R4)
         return gb::fail(APPFIS_GB_EINVAL, "star_r4: unknown tile %d", tile);
     int kz = zchunk <= 0 ? 0 : zchunk;  // 0: the tile's default (TMA-staged: 32-64 planes chosen for whole waves; 32 otherwise)
     cudaStream_t st = gb::as_stream(stream);

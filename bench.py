@@ -228,20 +228,21 @@ def cpu_app_samples():
             out[name] = {"error": "%s: %s" % (type(e).__name__, e)}
 
     def heat():
-        nx = ny = 1024
-        it = 400
-        f = W.heat2d_padded(nx, ny, 1.0, 42)
-        res, _ = O.run_ref("heat2d", [nx, ny, it, cores, 0.2, 1.0, "{in0}", "{out0}"],
+        c = W.HEAT2D
+        nx, ny, it = c["nx"], c["ny"], c["iters"]
+        f = W.heat2d_padded(nx, ny, c["top"], c["seed"])
+        res, _ = O.run_ref("heat2d", [nx, ny, it, cores, c["r"], c["top"], "{in0}", "{out0}"],
                            [np.ascontiguousarray(f[1:-1, 1:-1])], [(np.float32, 0)])
-        return nx * ny * it, res["seconds"], "1024x1024 FP32, %d of the 1000 iterations" % it
+        return nx * ny * it, res["seconds"], "the whole workload: %dx%d FP32, %d iterations" % (nx, ny, it)
 
     def himeno():
-        nx, ny, nz, it = 257, 257, 129, 10
+        c = W.HIMENO
+        nx, ny, nz, it = c["nx"], c["ny"], c["nz"], 10
         coef = W.himeno_coef(nx, ny, nz)
         p = W.himeno_p(nx, ny, nz)
-        res, _ = O.run_ref("himeno", [nx, ny, nz, it, cores, 0.8, "{in0}", "{in1}", "{out0}", "{out1}"],
+        res, _ = O.run_ref("himeno", [nx, ny, nz, it, cores, c["omega"], "{in0}", "{in1}", "{out0}", "{out1}"],
                            [coef, np.ascontiguousarray(p[1:-1, 1:-1, 1:-1])], [(np.float32, 0), (np.float64, 0)])
-        return nx * ny * nz * it, res["seconds"], "257x257x129 (a quarter of the z extent), %d sweeps" % it
+        return nx * ny * nz * it, res["seconds"], "the full %dx%dx%d grid, %d of the %d sweeps" % (nx, ny, nz, it, c["iters"])
 
     def fdtd():
         n, it = 512, 2
@@ -250,12 +251,22 @@ def cpu_app_samples():
         return n ** 3 * it, res["seconds"], "512^3 FP32, %d steps of the reference form (same 25-point reads)" % it
 
     def triton():
-        ny = nx = 1024
-        steps = 200
-        dem, h = W.triton_domain(ny, nx, 4242)
-        args = [nx, ny, cores, 10.0, 0.5, 1e-3, 0.035, 600.0, 600.0, 1.0, steps, "{in0}", "{in1}", "{out0}", "{out1}"]
-        res, _ = O.run_ref("triton", args, [dem, h], [(np.float64, 0), (np.float64, 0)])
-        return nx * ny * int(res["steps"]), res["seconds"], "one 1024x1024 domain, FP64, %d steps" % int(res["steps"])
+        # every fourth domain of the 32-domain batch (the same generator and seeds), each for its
+        # first 40 steps, through the reference's FP64 solver (its only precision)
+        c = W.TRITON
+        sizes = W.triton_sizes(c["n_domains"], c["side_lo"], c["side_hi"], c["seed"])
+        steps, cells, secs, picked = 40, 0, 0.0, []
+        for d in range(0, c["n_domains"], 4):
+            ny, nx = sizes[d]
+            dem, h = W.triton_domain(ny, nx, c["seed"] + 1000 * (d + 1))
+            args = [nx, ny, cores, c["dx"], c["courant"], c["hextra"], c["manning"], c["t_end"], c["t_end"], c["time_step"], steps,
+                    "{in0}", "{in1}", "{out0}", "{out1}"]
+            res, _ = O.run_ref("triton", args, [dem, h], [(np.float64, 0), (np.float64, 0)])
+            cells += nx * ny * int(res["steps"])
+            secs += res["seconds"]
+            picked.append("%dx%d" % (nx, ny))
+        return cells, secs, "domains %s of the 32-domain batch (every fourth), FP64, first %d steps each" % (
+            ", ".join(picked), steps)
 
     one("heat2d", heat)
     one("himeno", himeno)
@@ -729,6 +740,7 @@ def bench_fdtd(torch, gb, W, dev, sp, hbm):
     res = {}
     TMA_X4, AUTO = 8, 0
     names = {8: "star_r4_tma (4 x points / thread)", 9: "star_r4_tma (2 x points / thread)", 10: "star_r4_vec",
+             13: "star_r4_tma (4 x points x 4 rows / thread)",
              11: "star_r4_tb2 (two steps per launch, 64 x 16)", 12: "star_r4_tb2 (two steps per launch, 64 x 8)"}
 
     def run(x, y, x0, dt, iters, tile):
@@ -762,7 +774,7 @@ def bench_fdtd(torch, gb, W, dev, sp, hbm):
                          "traffic": profiled_traffic("star_r4_tma<float>"), "error_vs_fp64": err32}
     # one step of every tile (10 steps each, per-step time)
     tiles = {}
-    for tname, tid in (("tma_x4", 8), ("tma_x2", 9), ("tb2_64x16", 11), ("tb2_64x8", 12), ("vec", 10)):
+    for tname, tid in (("tma_x4", 8), ("tma_x4_4rows", 13), ("tma_x2", 9), ("tb2_64x16", 11), ("tb2_64x8", 12), ("vec", 10)):
         for dname, x, y, dt in (("fp32", a, b, 0), ("fp16", ha, hb, 3)):
             tiles["%s_%s_ms" % (tname, dname)] = steps_only(x, y, dt, tid)
     res["step_ms_by_tile"] = tiles

@@ -218,6 +218,7 @@ APPFIS_GB_API int appfis_gb_himeno_job(const float* coef_host, float* p_host, in
 #define APPFIS_GB_STAR_TB2 11    /* TMA-staged, TWO time steps per launch (64 x 16 output tile, step-1 values kept on
                                     chip); an odd last step runs in the TMA_X4 tile */
 #define APPFIS_GB_STAR_TB2_8 12  /* the same with a 64 x 8 output tile */
+#define APPFIS_GB_STAR_TMA_X4R4 13 /* TMA-staged 64 x 32 tile, 4 x points x 4 rows per thread */
 /* Replaces the per-step Execute3D(config, coeff, radius, cur, next) of the FDTD3d functor
  * (FDTD3d/src/fdtd3d_appfis.hpp:84-87,129-143) with radius 4 on a DUAL grid with a ghost halo of
  * width 4 (a, b: padded (nx+8) x (ny+8) x (nz+8), pitch >= nx+8, halo held at its values).

@@ -149,3 +149,18 @@ def test_mixed_error_both_kernels(gb, torch_cuda, pitch):
     mixed, gm = device_run(gb, torch_cuda, W.himeno_coef(nx, ny, nz), W.himeno_p(nx, ny, nz), iters, pitch, form=1)
     assert np.abs(mixed - p64).max() < 2.5e-4
     np.testing.assert_allclose(gm, g64, rtol=1e-2)
+
+
+@pytest.mark.parametrize("nx", [64, 66, 79, 129, 143, 200, 255])
+def test_mixed_tile_widths(gb, torch_cuda, nx):
+    """The TMA inner sweep takes 72-wide tiles where their whole tiles overhang columns 0..nx+1
+    less than 64-wide ones (nx 64, 66, 129, 143, 200) and 64-wide tiles otherwise (79, 255),
+    with one or several tiles across: p within the mixed form's 2.5e-4 of the FP64 oracle and
+    gosa within 1% per sweep."""
+    ny, nz, iters = 21, 30, 25
+    pitch = (nx + 2 + 7) // 8 * 8
+    p64, g64 = O.himeno(W.himeno_coef(nx, ny, nz, dtype=np.float64), W.himeno_p(nx, ny, nz, dtype=np.float64), iters, 0.8,
+                        dtype=np.float64)
+    mixed, gm = device_run(gb, torch_cuda, W.himeno_coef(nx, ny, nz), W.himeno_p(nx, ny, nz), iters, pitch, form=1)
+    assert np.abs(mixed - p64).max() < 2.5e-4
+    np.testing.assert_allclose(gm, g64, rtol=1e-2)

@@ -52,10 +52,10 @@ def test_reference_form_vs_oracle(gb, torch_cuda, nx, ny, nz, iters, ry, kz, pit
     assert np.array_equal(out, O.star_r4(f, iters, coeff=0.1))
 
 
-TMA_X4, TMA_X2, VEC = 8, 9, 10  # APPFIS_GB_STAR_* tiles
+TMA_X4, TMA_X2, VEC, TMA_X4R4 = 8, 9, 10, 13  # APPFIS_GB_STAR_* tiles
 
 
-@pytest.mark.parametrize("tile", [TMA_X4, TMA_X2, VEC])
+@pytest.mark.parametrize("tile", [TMA_X4, TMA_X2, VEC, TMA_X4R4])
 @pytest.mark.parametrize("nx,ny,nz,iters,kz,pitch", [(64, 70, 33, 2, 16, 72), (37, 29, 11, 3, 0, 48), (3, 17, 9, 2, 4, 12),
                                                      (95, 9, 20, 2, 0, 104)])
 def test_every_tile_reference_form(gb, torch_cuda, tile, nx, ny, nz, iters, kz, pitch):
@@ -64,7 +64,7 @@ def test_every_tile_reference_form(gb, torch_cuda, tile, nx, ny, nz, iters, kz, 
     assert np.array_equal(out, O.star_r4(f, iters, coeff=0.1))
 
 
-@pytest.mark.parametrize("tile", [TMA_X4, TMA_X2])
+@pytest.mark.parametrize("tile", [TMA_X4, TMA_X2, TMA_X4R4])
 def test_tma_tiles_fp16_weighted(gb, torch_cuda, tile):
     w = W.fdtd_weights()
     f = W.fdtd_padded(70, 33, 21, 17)
@@ -173,7 +173,17 @@ def test_autotuner_choice_is_used_and_exact(gb, torch_cuda):
     tile, kz, ms = ctypes.c_int(-1), ctypes.c_int(-1), ctypes.c_float(-1)
     gb.call("appfis_gb_star_r4_tune", a.data_ptr(), b.data_ptr(), 0, nx, ny, nz, pitch, 0, 0.1, None, ctypes.byref(tile),
             ctypes.byref(kz), ctypes.byref(ms), None)
-    assert tile.value in (TMA_X4, TMA_X2, TB2, TB2_8) and kz.value >= 0 and ms.value > 0
+    assert tile.value in (TMA_X4, TMA_X2, TB2, TB2_8, TMA_X4R4) and kz.value >= 0 and ms.value > 0
     assert torch.equal(a, torch.from_numpy(host).cuda())  # the input was not written
     out = run(gb, torch_cuda, f, 5, 0, 0.1, pitch=pitch, ry=0)
     assert np.array_equal(out, O.star_r4(f, 5, coeff=0.1))
+
+
+def test_four_row_tile_weighted_equals_two_row_tile(gb, torch_cuda):
+    """The 64 x 32 tile (4 rows per thread) does the 64 x 16 tile's per-point arithmetic: the
+    weighted form agrees bit for bit, ragged y included."""
+    w = W.fdtd_weights()
+    f = W.fdtd_padded(96, 45, 30, 29)
+    a = run(gb, torch_cuda, f, 5, 1, weights=w, pitch=104, ry=TMA_X4R4)
+    b = run(gb, torch_cuda, f, 5, 1, weights=w, pitch=104, ry=TMA_X4)
+    assert np.array_equal(a, b)
