@@ -75,7 +75,8 @@ def test_u8_vs_oracle(gb, torch_cuda, nx, ny, gens, rule):
 # buffer pairs before ping-ponging) plus a remainder.
 @pytest.mark.parametrize("nx,ny,gens", [(32, 1, 3), (32, 7, 5), (64, 40, 11), (1056, 66, 9), (2048, 130, 8), (96, 257, 21),
                                         (1056, 300, 33), (960, 70, 16), (32, 20, 16), (2048, 700, 48), (160, 1100, 17),
-                                        (256, 300, 80), (320, 140, 85), (128, 64, 112), (64, 520, 64)])
+                                        (256, 300, 80), (320, 140, 85), (128, 64, 112), (64, 520, 64), (992, 90, 32),
+                                        (1984, 40, 16), (1024, 33, 17)])
 @pytest.mark.parametrize("rule", [0, 1])
 def test_bits_vs_oracle(gb, torch_cuda, nx, ny, gens, rule):
     cells = W.gol_cells(nx, ny, 0.3, nx + 3 * ny)
@@ -109,6 +110,22 @@ def test_job_host_buffers(gb, torch_cuda, form):
     gb.call("appfis_gb_life_job", cells.ctypes.data, out.ctypes.data, nx, ny, gens, 0, form, ctypes.byref(pop))
     ref, _ = O.gol(cells, gens)
     assert np.array_equal(out, ref)
+    assert pop.value == int(ref.sum())
+
+
+@pytest.mark.parametrize("alias", [False, True])
+def test_job_page_locked_buffers(gb, torch_cuda, alias):
+    """Bit-packed form from page-locked host buffers (the bench's end-to-end case), also with the
+    output buffer over the input."""
+    torch = torch_cuda
+    nx, ny, gens = 2048, 130, 37
+    cells = W.gol_cells(nx, ny, 0.3, 78)
+    hin = torch.from_numpy(cells).pin_memory()
+    hout = hin if alias else torch.zeros_like(hin).pin_memory()
+    pop = ctypes.c_int64(-1)
+    gb.call("appfis_gb_life_job", hin.data_ptr(), hout.data_ptr(), nx, ny, gens, 0, 1, ctypes.byref(pop))
+    ref, _ = O.gol(cells, gens)
+    assert np.array_equal(hout.numpy(), ref)
     assert pop.value == int(ref.sum())
 
 
