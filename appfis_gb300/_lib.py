@@ -48,6 +48,7 @@ SIGNATURES = {
     "appfis_gb_heat2d_job": [_P, _i, _i, _i, _f, _f, _P],
     "appfis_gb_himeno": [_P, _P, _P, _i, _i, _i, _i, _i, _f, _P, _P, _P],
     "appfis_gb_himeno_mixed": [_P, _P, _P, _P, _i, _i, _i, _i, _i, _i, _f, _P, _P, _P],
+    "appfis_gb_himeno_mixed_ex": [_P, _P, _P, _P, _i, _i, _i, _i, _i, _i, _f, _i, _P, _P, _P],
     "appfis_gb_himeno_job": [_P, _P, _i, _i, _i, _i, _f, _i, _i, _P],
     "appfis_gb_star_r4": [_P, _P, _i, _i, _i, _i, _i, _i, _i, _f, _P, _i, _i, _P, _P],
     "appfis_gb_star_r4_tune": [_P, _P, _i, _i, _i, _i, _i, _i, _f, _P, _P, _P, _P, _P],

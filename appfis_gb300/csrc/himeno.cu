@@ -86,6 +86,73 @@ __device__ __forceinline__ void gosa_reduce(double v, double* __restrict__ parti
     }
 }
 
+// gosa_reduce for two sums at once (the two sweeps of one pass): partials[2b], partials[2b+1],
+// folded by the last block into out[0], out[1], each in block order.
+__device__ __forceinline__ void gosa_reduce2(double v1, double v2, double* __restrict__ partials, unsigned* __restrict__ ticket,
+                                             double* __restrict__ out)
+{
+    __shared__ double sh[2][32];
+    __shared__ bool last;
+    const int nthreads = blockDim.x * blockDim.y;
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v1 += __shfl_down_sync(0xffffffffu, v1, o);
+        v2 += __shfl_down_sync(0xffffffffu, v2, o);
+    }
+    if ((t & 31) == 0) {
+        sh[0][t >> 5] = v1;
+        sh[1][t >> 5] = v2;
+    }
+    __syncthreads();
+    const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned b = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    if (t < 32) {
+        v1 = t < (nthreads >> 5) ? sh[0][t] : 0.0;
+        v2 = t < (nthreads >> 5) ? sh[1][t] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            v1 += __shfl_down_sync(0xffffffffu, v1, o);
+            v2 += __shfl_down_sync(0xffffffffu, v2, o);
+        }
+        if (t == 0) {
+            partials[2 * b] = v1;
+            partials[2 * b + 1] = v2;
+            __threadfence();
+            last = atomicAdd(ticket, 1u) == nblk - 1;
+        }
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double w1 = 0.0, w2 = 0.0;
+    for (unsigned q = t; q < nblk; q += nthreads) {
+        w1 += ((volatile double*)partials)[2 * q];
+        w2 += ((volatile double*)partials)[2 * q + 1];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        w1 += __shfl_down_sync(0xffffffffu, w1, o);
+        w2 += __shfl_down_sync(0xffffffffu, w2, o);
+    }
+    __syncthreads();
+    if ((t & 31) == 0) {
+        sh[0][t >> 5] = w1;
+        sh[1][t >> 5] = w2;
+    }
+    __syncthreads();
+    if (t == 0) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int q = 0; q < (nthreads >> 5); q++) {
+            s1 += sh[0][q];
+            s2 += sh[1][q];
+        }
+        out[0] = s1;
+        out[1] = s2;
+        *ticket = 0;
+    }
+}
+
 // Per-thread sum of squares in two floats (hi + lo, ~48 significant bits): the square is split
 // exactly with an FMA and added with an exact two-sum, so a thread's few dozen terms stay within
 // ~1e-13 relative of the exact sum with FP32 instructions only (this part's FP64 rate is a small
@@ -431,12 +498,7 @@ __global__ void __launch_bounds__(RX* RY) himeno_tma(const __grid_constant__ Til
 // FP32, D as FP16) and the FP16 box of e plane k+2 (80 x 10, x origin = tile x - 8).  The threads
 // convert that box once into an FP32 ring slot (planes k-1 .. k+2 resident), so the 19 neighbour
 // reads of a pair are 19 FP32 shared loads (paired where the pair's columns are contiguous).
-constexpr int MX = 64, MY = 8, MXO = 8, MW = MX + 2 * MXO;
-constexpr int MEB = MW * (MY + 2) * 2;                  // FP16 e box bytes (1600)
-constexpr int MES = (MEB + 127) / 128 * 128;            // its slot
-constexpr int MCT = 10 * MX * MY * 2 + MX * MY * 4 + MX * MY * 2;  // per-point tiles of a plane (13312)
-constexpr int MSTG = MCT + MES;                         // one stage
-constexpr int MR32 = MW * (MY + 2);                     // floats per FP32 ring slot
+constexpr int MY = 8, MXO = 8;  // tile rows; x halo of the e box
 constexpr int MIX_S = 2;
 
 // The tile of width TW and its byte sizes.
@@ -455,6 +517,69 @@ __device__ __forceinline__ void e_box_to_f32(const unsigned char* src, float* ds
     const __half2* h = reinterpret_cast<const __half2*>(src);
     float2* d = reinterpret_cast<float2*>(dst);
     for (int q = t; q < MixTile<TW>::R32 / 2; q += TW / 2 * MY) d[q] = __half22float2(h[q]);
+}
+
+// The values of one e plane that a pair's 19-point sum takes from it when the plane is the one
+// above or below: the pair itself, the pairs at y +- 1 and the singles at x - 1 and x + 2.  As
+// the z-march advances, the set read for plane k+1 serves again as plane k's centre row and then
+// as plane k-1, so a step reads only plane k+1's set and plane k's four xy-diagonal singles.
+struct PlaneSet {
+    float2 c, yp, ym;
+    float l, r;
+};
+
+__device__ __forceinline__ PlaneSet plane_set(const float* __restrict__ b, int q, int W)
+{
+    PlaneSet p;
+    p.c = *reinterpret_cast<const float2*>(b + q);
+    p.yp = *reinterpret_cast<const float2*>(b + q + W);
+    p.ym = *reinterpret_cast<const float2*>(b + q - W);
+    p.l = b[q - 1];
+    p.r = b[q + 2];
+    return p;
+}
+
+// The xy-diagonal singles of the centre plane: (x-1, y+1), (x+2, y+1), (x-1, y-1), (x+2, y-1).
+__device__ __forceinline__ float4 plane_diag(const float* __restrict__ b, int q, int W)
+{
+    return make_float4(b[q + W - 1], b[q + W + 2], b[q - W - 1], b[q - W + 2]);
+}
+
+// One x pair of the FP16 defect-correction sweep from planes k-1 (m), k (z, with its diagonal
+// singles d) and k+1 (p), with the pair's coefficients co = a0 a1 a2 b0 b1 b2 c0 c1 c2 bnd, a3
+// and D: the new values v and ss = (v - e) / omega.  Terms with x neighbours take one value
+// from the next pair over, so their operands straddle register pairs: those are formed lane by
+// lane with scalar round-to-nearest operations (the same per-lane arithmetic as the packed ones).
+__device__ __forceinline__ void mix_pair(const PlaneSet& m, const PlaneSet& z, float4 d, const PlaneSet& p, const float2 (&co)[10],
+                                         float2 a3, float2 D, float2 wsplat, float2 isplat, float2& v, float2& ss)
+{
+    namespace f2 = gb::f2;
+    const float2 e0 = z.c, yp = z.yp, ym = z.ym, zp = p.c, zm = m.c;
+    const float e0l = z.l, e0r = z.r, ypl = d.x, ypr = d.y, yml = d.z, ymr = d.w;
+    const float zpl = p.l, zpr = p.r, zml = m.l, zmr = m.r;
+    // diagonal rows (dy, dz) = (+-1, +-1): centre pair only
+    const float2 ypzp = p.yp, ymzp = p.ym, ypzm = m.yp, ymzm = m.ym;
+    // F(+1, dy, dz) = (centre.y, right), F(-1, dy, dz) = (left, centre.x)
+    const float2 xp = make_float2(e0.y, e0r), xm = make_float2(e0l, e0.x);
+    const float2 xpyp = make_float2(yp.y, ypr), xmyp = make_float2(ypl, yp.x);
+    const float2 xpym = make_float2(ym.y, ymr), xmym = make_float2(yml, ym.x);
+    const float2 xpzp = make_float2(zp.y, zpr), xmzp = make_float2(zpl, zp.x);
+    const float2 xpzm = make_float2(zm.y, zmr), xmzm = make_float2(zml, zm.x);
+    float2 ne = make_float2(__fmul_rn(co[0].x, xp.x), __fmul_rn(co[0].y, xp.y));
+    ne = f2::fma(co[1], yp, ne);
+    ne = f2::fma(co[2], zp, ne);
+    const float2 txy = make_float2(__fsub_rn(__fsub_rn(xpyp.x, xpym.x), __fsub_rn(xmyp.x, xmym.x)),
+                                   __fsub_rn(__fsub_rn(xpyp.y, xpym.y), __fsub_rn(xmyp.y, xmym.y)));
+    ne = f2::fma(co[3], txy, ne);
+    ne = f2::fma(co[4], f2::sub(f2::sub(ypzp, ymzp), f2::sub(ypzm, ymzm)), ne);
+    const float2 txz = make_float2(__fsub_rn(__fsub_rn(xpzp.x, xmzp.x), __fsub_rn(xpzm.x, xmzm.x)),
+                                   __fsub_rn(__fsub_rn(xpzp.y, xmzp.y), __fsub_rn(xpzm.y, xmzm.y)));
+    ne = f2::fma(co[5], txz, ne);
+    ne = make_float2(__fmaf_rn(co[6].x, xm.x, ne.x), __fmaf_rn(co[6].y, xm.y, ne.y));
+    ne = f2::fma(co[7], ym, ne);
+    ne = f2::fma(co[8], zm, ne);
+    v = f2::add(f2::fma(f2::mul(wsplat, co[9]), f2::sub(f2::mul(a3, ne), e0), e0), D);
+    ss = f2::mul(f2::sub(v, e0), isplat);
 }
 
 // TW: tile width in x points (64 or 72: the launcher takes the one whose whole tiles cover the
@@ -513,6 +638,7 @@ __global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_consta
     const int cq = ty * MX + 2 * tx;          // this pair in a per-point tile (elements)
     const int q = (ty + 1) * MW + 2 * tx + MXO;  // this pair in a ring slot
     const float2 wsplat = f2::splat(omega), isplat = f2::splat(inv_omega);
+    PlaneSet pm, pz;  // planes k-1 and k of this pair (register queue)
     for (; k < k1; k++) {
         const int s = (k - k0) % S;
         if (!gb::tma::wait(&bar[s], (unsigned)((k - k0) / S) & 1u)) bad = true;
@@ -520,50 +646,21 @@ __global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_consta
         if (k == k0) {  // uniform
             for (int d = 0; d < 3; d++) e_box_to_f32<TW>(pro + d * MES, slot(k0 - 1 + d), t);
             __syncthreads();
+            pm = plane_set(slot(k0 - 1), q, MW);
+            pz = plane_set(slot(k0), q, MW);
         }
         e_box_to_f32<TW>(st + MCT, slot(k + 2), t);  // plane k+2 into the slot plane k-2 left
         {
-            const float* sm = slot(k - 1);
-            const float* s0 = slot(k);
-            const float* sp = slot(k + 1);
-            auto c2 = [&](const float* b, int dy) { return *reinterpret_cast<const float2*>(b + q + dy * MW); };
-            auto lf = [&](const float* b, int dy) { return b[q + dy * MW - 1]; };
-            auto rt = [&](const float* b, int dy) { return b[q + dy * MW + 2]; };
-            // rows with x neighbours: (dy, dz) = (0,0) (1,0) (-1,0) (0,1) (0,-1)
-            const float2 e0 = c2(s0, 0), yp = c2(s0, 1), ym = c2(s0, -1), zp = c2(sp, 0), zm = c2(sm, 0);
-            const float e0l = lf(s0, 0), e0r = rt(s0, 0), ypl = lf(s0, 1), ypr = rt(s0, 1), yml = lf(s0, -1), ymr = rt(s0, -1);
-            const float zpl = lf(sp, 0), zpr = rt(sp, 0), zml = lf(sm, 0), zmr = rt(sm, 0);
-            // diagonal rows (dy, dz) = (+-1, +-1): centre pair only
-            const float2 ypzp = c2(sp, 1), ymzp = c2(sp, -1), ypzm = c2(sm, 1), ymzm = c2(sm, -1);
-            // F(+1, dy, dz) = (centre.y, right), F(-1, dy, dz) = (left, centre.x)
-            const float2 xp = make_float2(e0.y, e0r), xm = make_float2(e0l, e0.x);
-            const float2 xpyp = make_float2(yp.y, ypr), xmyp = make_float2(ypl, yp.x);
-            const float2 xpym = make_float2(ym.y, ymr), xmym = make_float2(yml, ym.x);
-            const float2 xpzp = make_float2(zp.y, zpr), xmzp = make_float2(zpl, zp.x);
-            const float2 xpzm = make_float2(zm.y, zmr), xmzm = make_float2(zml, zm.x);
             float2 co[10];
 #pragma unroll
             for (int n = 0; n < 10; n++) co[n] = __half22float2(reinterpret_cast<const __half2*>(st + n * MX * MY * 2)[cq / 2]);
             const float2 a3 = reinterpret_cast<const float2*>(st + 10 * MX * MY * 2)[cq / 2];
             const float2 D = __half22float2(reinterpret_cast<const __half2*>(st + 10 * MX * MY * 2 + MX * MY * 4)[cq / 2]);
-            // a0 a1 a2 b0 b1 b2 c0 c1 c2 bnd.  Terms with x neighbours take one value from the
-            // next pair over, so their operands straddle register pairs: those are formed lane by
-            // lane with scalar round-to-nearest operations (the same per-lane arithmetic).
-            float2 ne = make_float2(__fmul_rn(co[0].x, xp.x), __fmul_rn(co[0].y, xp.y));
-            ne = f2::fma(co[1], yp, ne);
-            ne = f2::fma(co[2], zp, ne);
-            const float2 txy = make_float2(__fsub_rn(__fsub_rn(xpyp.x, xpym.x), __fsub_rn(xmyp.x, xmym.x)),
-                                           __fsub_rn(__fsub_rn(xpyp.y, xpym.y), __fsub_rn(xmyp.y, xmym.y)));
-            ne = f2::fma(co[3], txy, ne);
-            ne = f2::fma(co[4], f2::sub(f2::sub(ypzp, ymzp), f2::sub(ypzm, ymzm)), ne);
-            const float2 txz = make_float2(__fsub_rn(__fsub_rn(xpzp.x, xmzp.x), __fsub_rn(xpzm.x, xmzm.x)),
-                                           __fsub_rn(__fsub_rn(xpzp.y, xmzp.y), __fsub_rn(xpzm.y, xmzm.y)));
-            ne = f2::fma(co[5], txz, ne);
-            ne = make_float2(__fmaf_rn(co[6].x, xm.x, ne.x), __fmaf_rn(co[6].y, xm.y, ne.y));
-            ne = f2::fma(co[7], ym, ne);
-            ne = f2::fma(co[8], zm, ne);
-            const float2 v = f2::add(f2::fma(f2::mul(wsplat, co[9]), f2::sub(f2::mul(a3, ne), e0), e0), D);
-            float2 ss = f2::mul(f2::sub(v, e0), isplat);
+            const PlaneSet pp = plane_set(slot(k + 1), q, MW);
+            float2 v, ss;
+            mix_pair(pm, pz, plane_diag(slot(k), q, MW), pp, co, a3, D, wsplat, isplat, v, ss);
+            pm = pz;
+            pz = pp;
             const size_t cc = ((size_t)k * py + j) * pitch + xa;
             const __half2 hv = __float22half2_rn(v);
             if (!bad) {
@@ -588,6 +685,180 @@ __global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_consta
                 gb::tma::wait(&bar[(kk - k0) % S], (unsigned)((kk - k0) / S) & 1u, gb::tma::DRAIN_NS);
     }
     if (gosa) gosa_reduce(k < k1 ? __longlong_as_double(0x7ff8000000000000ll) : (double)g.x + (double)g.y, partials, ticket, gosa);
+}
+
+// ---------------------------------------------------------------- FP16 inner sweeps, two per pass
+// Two defect-correction sweeps per pass over a 56 x 8 output tile, so the ten FP16 coefficient
+// tiles, a3 and D of a plane (the 30 bytes a single sweep reads per point, 26 of them these) are
+// read once for both.  A stage brings them for plane q as 72 x 10 boxes (x from tile x - 8: the
+// tile and a one-point ring, x-aligned for the copy) and the FP16 e box of plane q+1 (72 x 12).
+// Sweep 1 computes e1 on the tile and its ring (30 x pairs from tile x - 2, 10 rows) from an FP32
+// ring of e planes; e1 is rounded to FP16 and back, as a stored sweep would round it, and is 0
+// outside the interior (the e fields' ghost cells are 0), so sweep 2, on the tile from an FP32
+// ring of e1 planes, gives the same bits as two single sweeps.  Step i (plane q = k0 - 1 + i)
+// runs sweep 1 of plane q, then sweep 2 of plane q - 1 with the previous step's stage: four
+// stages keep two planes in flight.  Both sweeps use mix_pair, the single sweep's arithmetic.
+constexpr int T2X = 56, T2Y = 8, T2W = 72;                     // output tile, box width
+constexpr int T2P1X = (T2X + 4) / 2, T2P1 = T2P1X * (T2Y + 2);  // sweep-1 pairs (30 x 10)
+constexpr int T2P2X = T2X / 2, T2P2 = T2P2X * T2Y;              // sweep-2 pairs (28 x 8)
+constexpr int T2NT = 320;                                       // threads (>= T2P1)
+constexpr int T2CBYTES = T2W * (T2Y + 2) * 2, T2ABYTES = T2W * (T2Y + 2) * 4, T2EBYTES = T2W * (T2Y + 4) * 2;
+constexpr int T2CB = (T2CBYTES + 127) / 128 * 128;              // FP16 per-point box slot
+constexpr int T2AB = (T2ABYTES + 127) / 128 * 128;              // a3 box slot
+constexpr int T2EB = (T2EBYTES + 127) / 128 * 128;              // e box slot
+constexpr int T2STG = 11 * T2CB + T2AB + T2EB;                  // 10 coefficients + D, a3, e of plane q+1
+constexpr int T2R0 = T2W * (T2Y + 4), T2R1 = T2W * (T2Y + 2);   // floats per e / e1 ring slot
+constexpr int T2R0B = (3 * T2R0 * 4 + 127) / 128 * 128;         // the two rings (3 slots each), 128-byte multiples
+constexpr int T2R1B = (3 * T2R1 * 4 + 127) / 128 * 128;
+constexpr int T2S = 4;
+constexpr int t2_smem() { return T2S * T2STG + T2R0B + T2R1B + 2 * T2EB + T2S * 8; }
+static_assert(T2STG % 128 == 0 && T2CB % 128 == 0 && T2AB % 128 == 0 && T2EB % 128 == 0, "copy destinations 128-byte aligned");
+static_assert(T2P1 <= T2NT && T2P2 <= T2NT, "thread count");
+
+__device__ __forceinline__ void e_box72_to_f32(const unsigned char* src, float* dst, int t)
+{
+    const __half2* h = reinterpret_cast<const __half2*>(src);
+    float2* d = reinterpret_cast<float2*>(dst);
+    for (int q = t; q < T2R0 / 2; q += T2NT) d[q] = __half22float2(h[q]);
+}
+
+__global__ void __launch_bounds__(T2NT, 2) himeno_mixed_tb2(const __grid_constant__ TileMaps maps, __half* __restrict__ eout, int nx,
+                                                            int ny, int nz, int pitch, int py, int kz, float omega, float inv_omega,
+                                                            double* __restrict__ partials, unsigned* __restrict__ ticket,
+                                                            double* __restrict__ gosa, unsigned* __restrict__ status)
+{
+    namespace f2 = gb::f2;
+    extern __shared__ __align__(128) unsigned char tsm[];
+    unsigned char* stages = tsm;
+    float* ring0 = reinterpret_cast<float*>(tsm + T2S * T2STG);
+    float* ring1 = reinterpret_cast<float*>(tsm + T2S * T2STG + T2R0B);
+    unsigned char* pro = tsm + T2S * T2STG + T2R0B + T2R1B;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(pro + 2 * T2EB);
+    const int t = threadIdx.x;
+    const int x0 = blockIdx.x * T2X, y0 = 1 + blockIdx.y * T2Y;
+    const int k0 = 1 + blockIdx.z * kz, k1 = min(k0 + kz, nz + 1);
+    const int qlo = k0 - 1, nst = k1 - k0 + 2;  // sweep 1 runs on planes qlo .. k1
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    if (gb::tma::smem_u32(tsm) & 127u) {
+        if (t == 0) atomicOr(status, (unsigned)gb::ST_SMEM_ALIGN);
+        if (gosa) gosa_reduce2(nan, nan, partials, ticket, gosa);
+        return;
+    }
+    if (t == 0) {
+#pragma unroll
+        for (int s = 0; s < T2S; s++) gb::tma::bar_init(&bar[s], 1);
+        gb::tma::fence_init();
+        for (int n = 0; n < 13; n++) gb::tma::prefetch_map(&maps.m[n]);
+    }
+    __syncthreads();
+    auto r0slot = [&](int pl) { return ring0 + ((unsigned)(pl - qlo + 1) % 3u) * T2R0; };  // e planes from qlo - 1
+    auto r1slot = [&](int pl) { return ring1 + ((unsigned)(pl - qlo) % 3u) * T2R1; };      // e1 planes from qlo
+    int last_issued = -1;  // thread 0 only
+    auto issue = [&](int i) {
+        const int s = i % T2S, q = qlo + i;
+        unsigned char* st = stages + s * T2STG;
+        last_issued = i;
+        gb::tma::arrive_expect(&bar[s], 11 * T2CBYTES + T2ABYTES + T2EBYTES + (i == 0 ? 2 * T2EBYTES : 0));
+        if (i == 0)
+            for (int d = 0; d < 2; d++) gb::tma::load_3d(pro + d * T2EB, &maps.m[12], x0 - 8, y0 - 2, qlo - 1 + d, &bar[s]);
+#pragma unroll
+        for (int n = 0; n < 10; n++) gb::tma::load_3d(st + n * T2CB, &maps.m[n], x0 - 8, y0 - 1, q, &bar[s]);
+        gb::tma::load_3d(st + 10 * T2CB, &maps.m[11], x0 - 8, y0 - 1, q, &bar[s]);         // D
+        gb::tma::load_3d(st + 11 * T2CB, &maps.m[10], x0 - 8, y0 - 1, q, &bar[s]);         // a3
+        gb::tma::load_3d(st + 11 * T2CB + T2AB, &maps.m[12], x0 - 8, y0 - 2, q + 1, &bar[s]);  // e of plane q+1
+    };
+    if (t == 0)
+        for (int i = 0; i < min(T2S, nst); i++) issue(i);
+
+    // sweep-1 pair of this thread (tile and ring), sweep-2 pair (tile)
+    const bool has1 = t < T2P1, has2 = t < T2P2;
+    const int p1x = t % T2P1X, p1y = t / T2P1X;
+    const int x1 = x0 - 2 + 2 * p1x, y1 = y0 - 1 + p1y;
+    const int c1 = p1y * T2W + 6 + 2 * p1x;        // in a per-point box and in an e1 slot
+    const int q1 = (p1y + 1) * T2W + 6 + 2 * p1x;  // in an e slot
+    const bool in1a = x1 >= 1 && x1 <= nx && y1 >= 1 && y1 <= ny, in1b = x1 + 1 >= 1 && x1 + 1 <= nx && y1 >= 1 && y1 <= ny;
+    const bool own1 = x1 >= x0 && x1 <= x0 + T2X - 2 && y1 >= y0 && y1 < y0 + T2Y;
+    const int p2x = t % T2P2X, p2y = t / T2P2X;
+    const int x2 = x0 + 2 * p2x, y2 = y0 + p2y;
+    const int c2i = (p2y + 1) * T2W + 8 + 2 * p2x;  // in a per-point box and in an e1 slot
+    const bool act2a = x2 >= 1 && x2 <= nx && y2 <= ny, act2b = x2 + 1 <= nx && y2 <= ny;
+    const float2 wsplat = f2::splat(omega), isplat = f2::splat(inv_omega);
+    auto load_pair = [&](const unsigned char* st, int c, float2 (&co)[10], float2& a3, float2& D) {
+#pragma unroll
+        for (int n = 0; n < 10; n++) co[n] = __half22float2(reinterpret_cast<const __half2*>(st + n * T2CB)[c / 2]);
+        D = __half22float2(reinterpret_cast<const __half2*>(st + 10 * T2CB)[c / 2]);
+        a3 = reinterpret_cast<const float2*>(st + 11 * T2CB)[c / 2];
+    };
+    float2 g1 = make_float2(0.0f, 0.0f), g2 = make_float2(0.0f, 0.0f);
+    PlaneSet m1, z1, m2, z2;  // register queues: e planes q-1, q (sweep 1); e1 planes k-1, k (sweep 2)
+    bool bad = false;
+    int i = 0;
+    for (; i < nst; i++) {
+        const int s = i % T2S, q = qlo + i;
+        if (!gb::tma::wait(&bar[s], (unsigned)(i / T2S) & 1u)) bad = true;
+        const unsigned char* st = stages + s * T2STG;
+        if (!bad) {
+            if (i == 0)
+                for (int d = 0; d < 2; d++) e_box72_to_f32(pro + d * T2EB, r0slot(qlo - 1 + d), t);
+            e_box72_to_f32(st + 11 * T2CB + T2AB, r0slot(q + 1), t);
+        }
+        // e planes q-1 .. q+1 are in; everyone is done with step i-1 (its sweep 2 read stage i-2)
+        if (__syncthreads_or(bad)) break;
+        if (t == 0 && i >= 2 && i + 2 < nst) issue(i + 2);
+        if (has1) {  // sweep 1, plane q
+            float2 co[10], a3, D, v, ss;
+            load_pair(st, c1, co, a3, D);
+            if (i == 0) {
+                m1 = plane_set(r0slot(q - 1), q1, T2W);
+                z1 = plane_set(r0slot(q), q1, T2W);
+            }
+            const PlaneSet p1 = plane_set(r0slot(q + 1), q1, T2W);
+            mix_pair(m1, z1, plane_diag(r0slot(q), q1, T2W), p1, co, a3, D, wsplat, isplat, v, ss);
+            m1 = z1;
+            z1 = p1;
+            const bool zin = q >= 1 && q <= nz;
+            const float2 vr = __half22float2(__float22half2_rn(v));  // as a stored sweep rounds it
+            *reinterpret_cast<float2*>(r1slot(q) + c1) = make_float2(zin && in1a ? vr.x : 0.0f, zin && in1b ? vr.y : 0.0f);
+            if (own1 && q >= k0 && q < k1) {
+                ss.x = in1a ? ss.x : 0.0f;
+                ss.y = in1b ? ss.y : 0.0f;
+                g1 = f2::fma(ss, ss, g1);
+            }
+        }
+        __syncthreads();  // e1 plane q is in
+        if (i >= 2 && has2) {  // sweep 2, plane q - 1 (k0 .. k1-1), with stage i-1
+            const int k = q - 1;
+            float2 co[10], a3, D, v, ss;
+            load_pair(stages + ((i - 1) % T2S) * T2STG, c2i, co, a3, D);
+            if (i == 2) {
+                m2 = plane_set(r1slot(k - 1), c2i, T2W);
+                z2 = plane_set(r1slot(k), c2i, T2W);
+            }
+            const PlaneSet p2 = plane_set(r1slot(k + 1), c2i, T2W);
+            mix_pair(m2, z2, plane_diag(r1slot(k), c2i, T2W), p2, co, a3, D, wsplat, isplat, v, ss);
+            m2 = z2;
+            z2 = p2;
+            const size_t cc = ((size_t)k * py + y2) * pitch + x2;
+            const __half2 hv = __float22half2_rn(v);
+            if (act2a && act2b) {
+                *reinterpret_cast<__half2*>(eout + cc) = hv;
+            } else {
+                if (act2a) eout[cc] = __low2half(hv);
+                if (act2b) eout[cc + 1] = __high2half(hv);
+            }
+            ss.x = act2a ? ss.x : 0.0f;
+            ss.y = act2b ? ss.y : 0.0f;
+            g2 = f2::fma(ss, ss, g2);
+        }
+    }
+    if (i < nst && t == 0) {  // a wait gave up: report and let the copies still in flight land
+        atomicOr(status, (unsigned)gb::ST_TMA_TIMEOUT);
+        for (int j = i; j <= last_issued; j++) gb::tma::wait(&bar[j % T2S], (unsigned)(j / T2S) & 1u, gb::tma::DRAIN_NS);
+    }
+    if (gosa) {
+        const bool ok = i == nst;
+        gosa_reduce2(ok ? (double)g1.x + (double)g1.y : nan, ok ? (double)g2.x + (double)g2.y : nan, partials, ticket, gosa);
+    }
 }
 
 // ---------------------------------------------------------------- TMA-staged correction pass
@@ -803,7 +1074,17 @@ int appfis_gb_himeno(const float* const* coef, float* p, float* wrk2, int nx, in
 int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, void* half_work, int nx, int ny, int nz,
                            int pitch, int iters, int period, float omega, double* dev_gosa, int* cur_index, void* stream)
 {
+    return appfis_gb_himeno_mixed_ex(coef, p, p_work, half_work, nx, ny, nz, pitch, iters, period, omega, 0, dev_gosa, cur_index,
+                                     stream);
+}
+
+int appfis_gb_himeno_mixed_ex(const float* const* coef, float* p, float* p_work, void* half_work, int nx, int ny, int nz,
+                              int pitch, int iters, int period, float omega, int sweeps_per_pass, double* dev_gosa, int* cur_index,
+                              void* stream)
+{
     if (!coef || !p || !p_work || !half_work || p == p_work) return gb::fail(APPFIS_GB_EINVAL, "himeno_mixed: null or aliased buffers");
+    if (sweeps_per_pass < 0 || sweeps_per_pass > 2)
+        return gb::fail(APPFIS_GB_EINVAL, "himeno_mixed: sweeps_per_pass %d (0, 1 or 2)", sweeps_per_pass);
     for (int n = 0; n < 12; n++)
         if (!coef[n]) return gb::fail(APPFIS_GB_EINVAL, "himeno_mixed: coefficient %d is null", n);
     GB_TRY(check_dims(nx, ny, nz, pitch));
@@ -860,9 +1141,43 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
                                      MY + 2));
         GB_TRY(gb::status_word(&status));
     }
+    // two sweeps per pass on request (measured slower than one per launch on every shape tried:
+    // the ring recompute and the second barrier per plane cost more than the bytes saved)
+    if (sweeps_per_pass == 2 && !use_tma)
+        return gb::fail(APPFIS_GB_EINVAL, "himeno_mixed: two sweeps per pass need 16-byte aligned rows (pitch %% 8 == 0)");
+    const bool two = use_tma && sweeps_per_pass == 2;
+    TileMaps t2maps[2];
+    dim3 t2grd(1, 1, 1);
+    int t2kz = 1;
+    if (two) {
+        const int py = ny + 2;
+        for (int n = 0; n < 10; n++)
+            GB_TRY(gb::tensor_map_3d(&t2maps[0].m[n], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, hf.c[n], nx + 2, py, nz + 2, pitch, py, T2W,
+                                     T2Y + 2));
+        GB_TRY(gb::tensor_map_3d(&t2maps[0].m[10], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, coef[3], nx + 2, py, nz + 2, pitch, py, T2W,
+                                 T2Y + 2));
+        GB_TRY(gb::tensor_map_3d(&t2maps[0].m[11], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, Dd, nx + 2, py, nz + 2, pitch, py, T2W, T2Y + 2));
+        t2maps[1] = t2maps[0];
+        for (int b = 0; b < 2; b++)
+            GB_TRY(gb::tensor_map_3d(&t2maps[b].m[12], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, E[b], nx + 2, py, nz + 2, pitch, py, T2W,
+                                     T2Y + 4));
+        constexpr int smem2 = t2_smem();
+        GB_CUDA(cudaFuncSetAttribute(himeno_mixed_tb2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2));
+        GB_CUDA(cudaFuncSetAttribute(himeno_mixed_tb2, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, himeno_mixed_tb2, T2NT, smem2) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        const int t2x = gb::ceil_div(nx + 1, T2X), t2y = gb::ceil_div(ny, T2Y);
+        t2kz = gb::wave_chunk(nz, 32, 64, (long long)t2x * t2y, (long long)per_sm * gb::sm_count(), 2);
+        t2grd = dim3(t2x, t2y, gb::ceil_div(nz, t2kz));
+    }
     double* rpartials = nullptr;
     unsigned* rticket = nullptr;
-    if (dev_gosa) GB_TRY(gosa_scratch(use_tma ? tgrd : rgrd, &rpartials, &rticket, st));
+    if (dev_gosa) {
+        const unsigned nb1 = use_tma ? tgrd.x * tgrd.y * tgrd.z : rgrd.x * rgrd.y * rgrd.z;
+        const unsigned nb2 = two ? 2 * t2grd.x * t2grd.y * t2grd.z : 0;
+        GB_TRY(gosa_scratch(dim3(std::max(nb1, nb2)), &rpartials, &rticket, st));
+    }
     float* P[2] = {p, p_work};
     // correction maps: [P buffer][e buffer]
     CorrMaps cmaps[2][2];
@@ -896,15 +1211,23 @@ int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, vo
     };
     correct();  // D from the initial P (e = 0), e restarted at 0
     const float inv_omega = 1.0f / omega;
-    for (int it = 0; it < iters; it++) {
-        if (use_tma) {
-            tkern<<<tgrd, tblk, tsmem, st>>>(tmaps[ec], E[1 - ec], nx, ny, nz, pitch, ny + 2, tkz, omega, inv_omega, rpartials, rticket,
-                                             dev_gosa ? dev_gosa + it : nullptr, status);
-        } else
-            himeno_ring<1><<<rgrd, rblk, 0, st>>>(cf, hf, E[ec], E[1 - ec], Dd, nx, ny, nz, pitch, ny + 2, HKZ, omega, inv_omega,
-                                                  rpartials, rticket, dev_gosa ? dev_gosa + it : nullptr);
+    for (int it = 0; it < iters;) {
+        const int left = std::min(iters - it, period - it % period);  // sweeps before the next correction
+        if (two && left >= 2) {
+            himeno_mixed_tb2<<<t2grd, T2NT, t2_smem(), st>>>(t2maps[ec], E[1 - ec], nx, ny, nz, pitch, ny + 2, t2kz, omega, inv_omega,
+                                                           rpartials, rticket, dev_gosa ? dev_gosa + it : nullptr, status);
+            it += 2;
+        } else {
+            if (use_tma)
+                tkern<<<tgrd, tblk, tsmem, st>>>(tmaps[ec], E[1 - ec], nx, ny, nz, pitch, ny + 2, tkz, omega, inv_omega, rpartials,
+                                                 rticket, dev_gosa ? dev_gosa + it : nullptr, status);
+            else
+                himeno_ring<1><<<rgrd, rblk, 0, st>>>(cf, hf, E[ec], E[1 - ec], Dd, nx, ny, nz, pitch, ny + 2, HKZ, omega, inv_omega,
+                                                      rpartials, rticket, dev_gosa ? dev_gosa + it : nullptr);
+            it += 1;
+        }
         ec = 1 - ec;
-        if ((it + 1) % period == 0 || it + 1 == iters) correct();
+        if (it % period == 0 || it == iters) correct();
     }
     GB_TRY(gb::launched("himeno_mixed"));
     if (cur_index) *cur_index = pc;

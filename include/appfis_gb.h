@@ -202,6 +202,15 @@ APPFIS_GB_API int appfis_gb_himeno(const float* const* coef, float* p, float* wr
 APPFIS_GB_API int appfis_gb_himeno_mixed(const float* const* coef, float* p, float* p_work, void* half_work, int nx, int ny,
                                          int nz, int pitch, int iters, int period, float omega, double* dev_gosa,
                                          int* cur_index, void* stream);
+/* appfis_gb_himeno_mixed with the number of inner sweeps per launch: 1 (the default, also for
+ * 0) or 2: the coefficient, a3 and D tiles of a plane read once for two sweeps, the same bits as
+ * two single sweeps (gosa summed in another order); it needs 16-byte aligned rows (pitch a
+ * multiple of 8; EINVAL otherwise), and a period with an odd count of inner sweeps ends with a
+ * single sweep.  On GB300 the two-sweep form is slower at every size measured (its one-point
+ * ring is recomputed and each plane takes a second barrier), so it is an option, not a default. */
+APPFIS_GB_API int appfis_gb_himeno_mixed_ex(const float* const* coef, float* p, float* p_work, void* half_work, int nx,
+                                            int ny, int nz, int pitch, int iters, int period, float omega,
+                                            int sweeps_per_pass, double* dev_gosa, int* cur_index, void* stream);
 /* Whole run from host: coef_host = 12 dense padded fields back to back, p_host = dense padded p
  * (in place).  form 0 = plain FP32, 1 = defect correction with `period`.  gosa_host: `iters`
  * doubles or NULL. */

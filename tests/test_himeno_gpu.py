@@ -8,6 +8,7 @@ import os
 import numpy as np
 import pytest
 
+from appfis_gb300 import _lib
 from appfis_gb300 import workloads as W
 from oracle import oracle as O
 
@@ -89,8 +90,9 @@ def test_mixed_defect_correction_error(gb, torch_cuda):
     np.testing.assert_allclose(gp, g64, rtol=1e-4)
 
 
-def device_run(gb, torch, coef, p, iters, pitch, form=0, period=20, omega=0.8):
-    """Runs the device entry point on fields whose rows are padded to `pitch` elements."""
+def device_run(gb, torch, coef, p, iters, pitch, form=0, period=20, omega=0.8, spp=0):
+    """Runs the device entry point on fields whose rows are padded to `pitch` elements (spp: the
+    mixed form's inner sweeps per launch, 0 = its default of one)."""
     nz, ny, nx = p.shape[0] - 2, p.shape[1] - 2, p.shape[2] - 2
     hp = np.zeros((nz + 2, ny + 2, pitch), dtype=np.float32)
     hp[:, :, : nx + 2] = p
@@ -107,8 +109,8 @@ def device_run(gb, torch, coef, p, iters, pitch, form=0, period=20, omega=0.8):
                 ctypes.byref(ci), None)
     else:
         half = torch.empty(13 * hp.size, dtype=torch.float16, device="cuda")
-        gb.call("appfis_gb_himeno_mixed", ptrs, a.data_ptr(), b.data_ptr(), half.data_ptr(), nx, ny, nz, pitch, iters,
-                period, omega, g.data_ptr(), ctypes.byref(ci), None)
+        gb.call("appfis_gb_himeno_mixed_ex", ptrs, a.data_ptr(), b.data_ptr(), half.data_ptr(), nx, ny, nz, pitch, iters,
+                period, omega, spp, g.data_ptr(), ctypes.byref(ci), None)
     gb.call("appfis_gb_stream_sync", None)
     out = (a if ci.value == 0 else b).cpu().numpy()[:, :, : nx + 2]
     return out, g.cpu().numpy()[:iters]
@@ -164,3 +166,25 @@ def test_mixed_tile_widths(gb, torch_cuda, nx):
     mixed, gm = device_run(gb, torch_cuda, W.himeno_coef(nx, ny, nz), W.himeno_p(nx, ny, nz), iters, pitch, form=1)
     assert np.abs(mixed - p64).max() < 2.5e-4
     np.testing.assert_allclose(gm, g64, rtol=1e-2)
+
+
+@pytest.mark.parametrize("nx,ny,nz,iters,period", [(1, 1, 1, 4, 20), (30, 7, 5, 6, 20), (55, 9, 33, 7, 3), (56, 16, 70, 9, 4),
+                                                   (57, 17, 64, 10, 20), (129, 23, 129, 12, 5), (257, 33, 40, 8, 20)])
+def test_mixed_two_sweeps_per_pass_bit_identical(gb, torch_cuda, nx, ny, nz, iters, period):
+    """Two inner sweeps per launch (56 x 8 tiles with the one-point ring recomputed, level-1
+    values rounded through FP16) against one sweep per launch: p bit-identical after corrections
+    and odd leftovers (periods of 3 and 5 end with a single sweep), gosa within 1e-5 (the same
+    per-point squares summed in another grouping); ragged x tiles, y not a multiple of 8, z
+    chunks of one plane."""
+    pitch = (nx + 2 + 7) // 8 * 8
+    coef, p = W.himeno_coef(nx, ny, nz, seed=nx + 5 * nz), W.himeno_p(nx, ny, nz)
+    one, g1 = device_run(gb, torch_cuda, coef, p, iters, pitch, form=1, period=period, spp=1)
+    two, g2 = device_run(gb, torch_cuda, coef, p, iters, pitch, form=1, period=period, spp=2)
+    assert np.array_equal(one, two)
+    np.testing.assert_allclose(g2, g1, rtol=1e-5, atol=0)
+
+
+def test_mixed_two_sweeps_needs_aligned_rows(gb, torch_cuda):
+    nx, ny, nz = 13, 5, 4
+    with pytest.raises(_lib.AppfisError):
+        device_run(gb, torch_cuda, W.himeno_coef(nx, ny, nz), W.himeno_p(nx, ny, nz), 2, nx + 2, form=1, spp=2)
