@@ -600,6 +600,9 @@ __global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_consta
     unsigned char* pro = tsm + S * MSTG + 4 * MR32 * 4;
     uint64_t* bar = reinterpret_cast<uint64_t*>(pro + 3 * MES);
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * (MX / 2) + tx;
+    // the copies are issued by the last warp's first thread: the e box conversion leaves that
+    // warp the fewest pairs, so the issue work does not delay the plane's slowest warp
+    const int issuer = MX / 2 * MY - 32;
     const int x0 = blockIdx.x * MX, y0 = 1 + blockIdx.y * MY;
     const int xa = x0 + 2 * tx, j = y0 + ty;
     const int k0 = 1 + blockIdx.z * kz, k1 = min(k0 + kz, nz + 1);
@@ -609,7 +612,7 @@ __global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_consta
         if (gosa) gosa_reduce(__longlong_as_double(0x7ff8000000000000ll), partials, ticket, gosa);
         return;
     }
-    if (t == 0) {
+    if (t == issuer) {
 #pragma unroll
         for (int s = 0; s < S; s++) gb::tma::bar_init(&bar[s], 1);
         gb::tma::fence_init();
@@ -629,7 +632,7 @@ __global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_consta
         gb::tma::load_3d(st + 10 * MX * MY * 2 + MX * MY * 4, &maps.m[11], x0, y0, k, &bar[s]);
         gb::tma::load_3d(st + MCT, &maps.m[12], x0 - MXO, y0 - 1, k + 2, &bar[s]);
     };
-    if (t == 0)
+    if (t == issuer)
         for (int k = k0; k < min(k0 + S, k1); k++) issue(k);
 
     float2 g = make_float2(0.0f, 0.0f);
@@ -677,7 +680,7 @@ __global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_consta
         }
         // everyone is done with stage s, the slot of plane k-1 and the conversions of plane k+2
         if (__syncthreads_or(bad)) break;
-        if (t == 0 && k + S < k1) issue(k + S);
+        if (t == issuer && k + S < k1) issue(k + S);
     }
     if (k < k1 && t == 0) {  // a wait gave up: report and let the copies still in flight land
         atomicOr(status, (unsigned)gb::ST_TMA_TIMEOUT);
@@ -734,7 +737,7 @@ __global__ void __launch_bounds__(T2NT, 2) himeno_mixed_tb2(const __grid_constan
     float* ring1 = reinterpret_cast<float*>(tsm + T2S * T2STG + T2R0B);
     unsigned char* pro = tsm + T2S * T2STG + T2R0B + T2R1B;
     uint64_t* bar = reinterpret_cast<uint64_t*>(pro + 2 * T2EB);
-    const int t = threadIdx.x;
+    const int t = threadIdx.x, issuer = T2NT - 32;  // the copies: the last warp (no sweep-2 pairs)
     const int x0 = blockIdx.x * T2X, y0 = 1 + blockIdx.y * T2Y;
     const int k0 = 1 + blockIdx.z * kz, k1 = min(k0 + kz, nz + 1);
     const int qlo = k0 - 1, nst = k1 - k0 + 2;  // sweep 1 runs on planes qlo .. k1
@@ -744,7 +747,7 @@ __global__ void __launch_bounds__(T2NT, 2) himeno_mixed_tb2(const __grid_constan
         if (gosa) gosa_reduce2(nan, nan, partials, ticket, gosa);
         return;
     }
-    if (t == 0) {
+    if (t == issuer) {
 #pragma unroll
         for (int s = 0; s < T2S; s++) gb::tma::bar_init(&bar[s], 1);
         gb::tma::fence_init();
@@ -753,7 +756,7 @@ __global__ void __launch_bounds__(T2NT, 2) himeno_mixed_tb2(const __grid_constan
     __syncthreads();
     auto r0slot = [&](int pl) { return ring0 + ((unsigned)(pl - qlo + 1) % 3u) * T2R0; };  // e planes from qlo - 1
     auto r1slot = [&](int pl) { return ring1 + ((unsigned)(pl - qlo) % 3u) * T2R1; };      // e1 planes from qlo
-    int last_issued = -1;  // thread 0 only
+    int last_issued = -1;  // the issuing thread only
     auto issue = [&](int i) {
         const int s = i % T2S, q = qlo + i;
         unsigned char* st = stages + s * T2STG;
@@ -767,7 +770,7 @@ __global__ void __launch_bounds__(T2NT, 2) himeno_mixed_tb2(const __grid_constan
         gb::tma::load_3d(st + 11 * T2CB, &maps.m[10], x0 - 8, y0 - 1, q, &bar[s]);         // a3
         gb::tma::load_3d(st + 11 * T2CB + T2AB, &maps.m[12], x0 - 8, y0 - 2, q + 1, &bar[s]);  // e of plane q+1
     };
-    if (t == 0)
+    if (t == issuer)
         for (int i = 0; i < min(T2S, nst); i++) issue(i);
 
     // sweep-1 pair of this thread (tile and ring), sweep-2 pair (tile)
@@ -804,7 +807,7 @@ __global__ void __launch_bounds__(T2NT, 2) himeno_mixed_tb2(const __grid_constan
         }
         // e planes q-1 .. q+1 are in; everyone is done with step i-1 (its sweep 2 read stage i-2)
         if (__syncthreads_or(bad)) break;
-        if (t == 0 && i >= 2 && i + 2 < nst) issue(i + 2);
+        if (t == issuer && i >= 2 && i + 2 < nst) issue(i + 2);
         if (has1) {  // sweep 1, plane q
             float2 co[10], a3, D, v, ss;
             load_pair(st, c1, co, a3, D);
@@ -851,7 +854,7 @@ __global__ void __launch_bounds__(T2NT, 2) himeno_mixed_tb2(const __grid_constan
             g2 = f2::fma(ss, ss, g2);
         }
     }
-    if (i < nst && t == 0) {  // a wait gave up: report and let the copies still in flight land
+    if (i < nst && t == issuer) {  // a wait gave up: report and let the copies still in flight land
         atomicOr(status, (unsigned)gb::ST_TMA_TIMEOUT);
         for (int j = i; j <= last_issued; j++) gb::tma::wait(&bar[j % T2S], (unsigned)(j / T2S) & 1u, gb::tma::DRAIN_NS);
     }
