@@ -38,7 +38,7 @@ struct SrcDev {
 
 struct Ctl {
     int src_lo[MAXD];     // hydrograph row of each domain's sources (kept across steps)
-    unsigned long long dtbits[2][MAXD];
+    unsigned long long dtbits[3][MAXD];  // two-phase kernel: by step parity; fused kernel: by step mod 3
     double simtime[2][MAXD];
     int pid[2][MAXD];
     int steps[2][MAXD];
@@ -118,14 +118,20 @@ __device__ __forceinline__ T typed(double d, float f)
         return d;
 }
 
-__device__ __forceinline__ double step_dt(const Ctl* ctl, int cur, int d, const Params& p, double big)
+// The dt of domain d's step from its CFL minimum in dtbits[slot] and the step's scalars [cur].
+__device__ __forceinline__ double step_dt_at(const Ctl* ctl, int slot, int cur, int d, const Params& p, double big)
 {
-    double dt = __longlong_as_double((long long)ctl->dtbits[cur][d]);
+    double dt = __longlong_as_double((long long)ctl->dtbits[slot][d]);
     if (dt >= big - 1.0) dt = p.time_step;
     const double st = ctl->simtime[cur][d];
     const double next_print = p.print_interval * (ctl->pid[cur][d] + 1);
     if (st + dt > next_print) dt = next_print - st;
     return dt;
+}
+
+__device__ __forceinline__ double step_dt(const Ctl* ctl, int cur, int d, const Params& p, double big)
+{
+    return step_dt_at(ctl, cur, cur, d, p, big);
 }
 
 __device__ __forceinline__ bool is_active(const Ctl* ctl, int cur, int d, const Params& p)
@@ -140,13 +146,15 @@ __device__ __forceinline__ bool is_active(const Ctl* ctl, int cur, int d, const 
 // warp has several rows of loads in flight instead of one.
 constexpr int FA_ROWS = 4;
 
-template <class T>
-__device__ void phase_a(const Dom<T> D, Ctl* ctl, int cur, int d, long long local, int b, bool fix, bool want_dt,
+// SC, LO: the strip geometry (SC columns per strip on lanes LO .. LO+SC-1; the two-phase kernel's
+// 30 on lanes 1..30, the fused kernel's 28 on lanes 2..29); the CFL minimum goes to dtbits[slot].
+template <class T, int SC = SCOLS, int LO = 1>
+__device__ void phase_a(const Dom<T> D, Ctl* ctl, int slot, int d, long long local, int b, bool fix, bool want_dt,
                         const Params& p)
 {
     const int lane = threadIdx.x & 31;
     const int loc = (int)local, sy = loc / D.strips_x, sx = loc - sy * D.strips_x;  // 32-bit: a domain has < 2^31 strips
-    const int i = sx * SCOLS + lane;  // lanes 1..SCOLS: the strip's interior columns
+    const int i = sx * SC + lane - LO + 1;  // lanes LO..LO+SC-1: the strip's interior columns
     const int j0 = 1 + sy * ROWS, j1 = min(j0 + ROWS, D.ny + 1);
     const T* __restrict__ h = D.h[b];
     T* __restrict__ qx = D.qx[b];
@@ -156,7 +164,7 @@ __device__ void phase_a(const Dom<T> D, Ctl* ctl, int cur, int d, long long loca
     const T hextra = typed<T>(p.hextra, p.fhextra), E = K<T>::dry(), G = K<T>::g();
     const T dx = typed<T>(p.dx, p.fdx), cn = typed<T>(p.cn, p.fcn);
     T mn = K<T>::big();  // min in T (exact), widened once per warp: no per-cell FP64 work in float
-    if (lane >= 1 && lane <= SCOLS && i <= D.nx) {
+    if (lane >= LO && lane < LO + SC && i <= D.nx) {
         for (int jb = j0; jb < j1; jb += FA_ROWS) {
             T hv[FA_ROWS], qxv[FA_ROWS], qyv[FA_ROWS];
 #pragma unroll
@@ -200,7 +208,7 @@ __device__ void phase_a(const Dom<T> D, Ctl* ctl, int cur, int d, long long loca
             mn = other < mn ? other : mn;
         }
         if (lane == 0 && mn < K<T>::big())
-            atomicMin(&ctl->dtbits[cur][d], (unsigned long long)__double_as_longlong((double)mn));
+            atomicMin(&ctl->dtbits[slot][d], (unsigned long long)__double_as_longlong((double)mn));
     }
 }
 
@@ -497,6 +505,208 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
     }
 }
 
+// ---------------------------------------------------------------- fused step (full sweep)
+// One pass per step: each warp updates its strip and the one-cell ring around it (the ring cells
+// are updated again, with the same arithmetic, by the strips that own them), so the wet/dry fix
+// of its own cells, which reads the updated depth and the bed of their four neighbours, and the
+// CFL dt of the next step follow in the same pass; the two-phase kernel's separate read of the
+// state for fix and dt (16 of its 48 bytes per cell-step) and one grid barrier per step go away.
+// Strips are FCOLS columns: lane l holds column FCOLS*sx + l - 1, lanes 1..30 update their cell,
+// lanes 2..29 own it (write it, fix it, take its dt).  The strip's rows and the row above and
+// below it are updated; row r-1 is fixed once row r is.  The fields are bit-identical to the
+// two-phase kernel's: the same face, update, fix and dt functions of the same values.
+constexpr int FCOLS = 28;
+
+template <class T>
+__device__ void phase_bf(const Dom<T> D, long long local, int b, T dt, const Params& p, unsigned long long* dt_next)
+{
+    const int lane = threadIdx.x & 31;
+    const int loc = (int)local, sy = loc / D.strips_x, sx = loc - sy * D.strips_x;  // 32-bit: a domain has < 2^31 strips
+    const int i = sx * FCOLS + lane - 1;
+    const int j0 = 1 + sy * ROWS, j1 = min(j0 + ROWS, D.ny + 1);  // owned rows j0 .. j1-1
+    const int nx = D.nx, ny = D.ny, px = D.px;
+    const bool col = i >= 0 && i <= nx + 1;                            // a column of the padded domain
+    const bool upd = lane >= 1 && lane <= 30 && i >= 1 && i <= nx;     // updates its cell
+    const bool own = lane >= 2 && lane <= 29 && i <= nx;               // owns it
+    const bool xface = lane <= 30 && i >= 0 && i <= nx;                // face i|i+1
+    const T dx = typed<T>(p.dx, p.fdx), hextra = typed<T>(p.hextra, p.fhextra), cn = typed<T>(p.cn, p.fcn);
+    const T one = T(1), zero = T(0), E = K<T>::dry(), G = K<T>::g();
+    const T* __restrict__ h = D.h[b];
+    const T* __restrict__ qx = D.qx[b];
+    const T* __restrict__ qy = D.qy[b];
+    const T* __restrict__ dem = D.dem;
+    const T* __restrict__ n2 = D.n2;
+    T* __restrict__ ho_ = D.h[1 - b];
+    T* __restrict__ qxo_ = D.qx[1 - b];
+    T* __restrict__ qyo_ = D.qy[1 - b];
+    const Raw<T> zr = {zero, zero, zero, zero};
+    auto raw = [&](int r) -> Raw<T> {  // state of row r (zero outside the padded domain)
+        if (!col || r < 0 || r > ny + 1) return zr;
+        const size_t c = (size_t)r * px + i;
+        return Raw<T>{h[c], qx[c], qy[c], dem[c]};
+    };
+    const int ra = j0 - 1, rb = j1;  // rows updated (those outside 1..ny keep their state)
+    Cell<T> cj = cell_of(raw(ra));
+    Raw<T> rn = raw(ra + 1);
+    T ycar[3] = {zero, zero, zero};  // rhs0 Y part of row r (from face r|r-1)
+    bool ywet = false;
+    if (upd && ra >= 1) {
+        const Cell<T> cm = cell_of(raw(ra - 1));
+        T r2[3];
+        ywet = face<T>(cj, cm, zero, one, dx, dt, hextra, ycar, r2);
+    }
+    T h2 = zero, z2 = zero;                         // row r-2: updated depth, bed
+    T h1 = zero, qx1 = zero, qy1 = zero, z1 = zero;  // row r-1: updated state, bed
+    T mn = K<T>::big();
+    for (int r = ra; r <= rb; r++) {
+        const Raw<T> rnn = r + 2 <= rb + 1 ? raw(r + 2) : zr;  // prefetch
+        const bool rin = r >= 1 && r <= ny;
+        const T n2v = upd && rin ? n2[(size_t)r * px + i] : zero;
+        const Cell<T> cn_ = cell_of(rn);
+        // X face i|i+1 of row r: rhs0 of cell i, rhs1 of cell i+1 (the next lane)
+        const Cell<T> right = shfl_cell(cj, 1, true);
+        T xr1[3] = {zero, zero, zero}, xr2[3] = {zero, zero, zero};
+        bool xwet = false;
+        if (xface && rin) xwet = face<T>(cj, right, one, zero, dx, dt, hextra, xr1, xr2);
+        T lr[3];
+        lr[0] = __shfl_up_sync(0xffffffffu, xr2[0], 1);
+        lr[1] = __shfl_up_sync(0xffffffffu, xr2[1], 1);
+        lr[2] = __shfl_up_sync(0xffffffffu, xr2[2], 1);
+        const bool lwet = __shfl_up_sync(0xffffffffu, (int)xwet, 1) != 0;
+        // Y face r+1|r: id1 = row r+1, id2 = row r (row r's rhs1 and row r+1's rhs0)
+        T yn1[3] = {zero, zero, zero}, yr2[3] = {zero, zero, zero};
+        bool ynwet = false;
+        if (upd && r >= 0 && r <= ny) ynwet = face<T>(cn_, cj, zero, one, dx, dt, hextra, yn1, yr2);
+        T hn = cj.h, qxn = cj.qx, qyn = cj.qy;
+        if (upd && rin) {
+            T r0[3], r1[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                r0[k] = xwet ? xr1[k] : zero;
+                if (ywet) r0[k] = r0[k] + ycar[k];
+                r1[k] = lwet ? lr[k] : zero;
+                if (ynwet) r1[k] = r1[k] + yr2[k];
+            }
+            update<T>(cj.h, cj.qx, cj.qy, n2v, r0, r1, dt, hextra, hn, qxn, qyn);
+        }
+        // row r-1, one of the strip's own rows: wet/dry fix (triton_appfis.hpp:1095-1112) on the
+        // updated state, then its CFL dt (:567-586), then the write
+        if (r - 1 >= j0 && r - 1 < j1) {
+            const T hL = __shfl_up_sync(0xffffffffu, h1, 1), hR = __shfl_down_sync(0xffffffffu, h1, 1);
+            const T zL = __shfl_up_sync(0xffffffffu, z1, 1), zR = __shfl_down_sync(0xffffffffu, z1, 1);
+            if (own) {
+                T qxr = qx1, qyr = qy1;
+                if (h1 > hextra) {
+                    const T lvl = h1 + z1;
+                    if (((lvl < zR) && (hR < E)) || ((lvl < zL) && (hL < E))) qxr = zero;
+                    if (((lvl < z2) && (h2 < E)) || ((lvl < cj.z) && (hn < E))) qyr = zero;
+                    const T dtx = dx / (fabs(qxr / h1) + sqrt(G * h1));
+                    const T dty = dx / (fabs(qyr / h1) + sqrt(G * h1));
+                    const T v = dtx < dty ? cn * dtx : cn * dty;
+                    mn = v < mn ? v : mn;
+                }
+                const size_t c1 = (size_t)(r - 1) * px + i;
+                ho_[c1] = h1;
+                qxo_[c1] = qxr;
+                qyo_[c1] = qyr;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) ycar[k] = yn1[k];
+        ywet = ynwet;
+        h2 = h1;
+        z2 = z1;
+        h1 = hn;
+        qx1 = qxn;
+        qy1 = qyn;
+        z1 = cj.z;
+        cj = cn_;
+        rn = rnn;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const T other = __shfl_down_sync(0xffffffffu, mn, o);
+        mn = other < mn ? other : mn;
+    }
+    if (lane == 0 && mn < K<T>::big()) atomicMin(dt_next, (unsigned long long)__double_as_longlong((double)mn));
+}
+
+// The fused persistent kernel (full sweep, no point sources): a dt-only pass over the initial
+// state, then one pass and one grid barrier per step.  The per-domain CFL minimum of step n is
+// accumulated in dtbits[n % 3] during step n-1, read at the start of step n, and the slot of
+// step n+2 is reset by block 0 during step n (nobody reads or writes it then).
+template <class T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1) flood_fused(const Dom<T>* __restrict__ gdoms, Ctl* ctl,
+                                                                                          Params p)
+{
+    __shared__ Dom<T> doms[MAXD];
+    __shared__ DomCtl<T> dc;
+    for (int k = threadIdx.x; k < p.ndom; k += blockDim.x) doms[k] = gdoms[k];
+    __syncthreads();
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const double big = (double)K<T>::big();
+    // dt of step 0 from the initial state (no fix before the first step)
+    if (threadIdx.x < p.ndom) dc.flags[threadIdx.x] = is_active(ctl, 0, threadIdx.x, p) ? 4 : 0;
+    __syncthreads();
+    for_strips(&ctl->ticket[0], warp, nwarps, p.total_strips, lane, [&](long long s) {
+        const int d = find_domain(doms, p.ndom, s);
+        if (dc.flags[d] & 4) phase_a<T, FCOLS, 2>(doms[d], ctl, 0, d, s - doms[d].strip0, ctl->steps[0][d] & 1, false, true, p);
+    });
+    if (!grid_barrier(ctl, p.spin_limit, (int)blockIdx.x == p.stall_cta)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ticket[0] = 0;
+    for (int n = 0;; n++) {
+        const int cur = n & 1, ds = n % 3;
+        int active = 0;
+        if (threadIdx.x < p.ndom) {
+            const int d = threadIdx.x;
+            active = is_active(ctl, cur, d, p) ? 1 : 0;
+            const double dt = active ? step_dt_at(ctl, ds, cur, d, p, big) : 0.0;
+            const bool run = active && dt > 1e-9 * p.time_step;
+            dc.dt[d] = (T)dt;
+            dc.flags[d] = (unsigned char)((ctl->steps[cur][d] & 1) | (run ? 4 : 0));
+        }
+        if (!__syncthreads_or(active)) {
+            if (blockIdx.x == 0 && threadIdx.x == 0)  // leave the final scalars in both halves
+                for (int d = 0; d < p.ndom; d++) {
+                    ctl->simtime[1 - cur][d] = ctl->simtime[cur][d];
+                    ctl->pid[1 - cur][d] = ctl->pid[cur][d];
+                    ctl->steps[1 - cur][d] = ctl->steps[cur][d];
+                }
+            return;
+        }
+        const int dn = (n + 1) % 3;
+        for_strips(&ctl->ticketb[cur], warp, nwarps, p.total_strips, lane, [&](long long s) {
+            const int d = find_domain(doms, p.ndom, s);
+            const int f = dc.flags[d];
+            if (f & 4) phase_bf<T>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p, &ctl->dtbits[dn][d]);
+        });
+        if (blockIdx.x == 0 && threadIdx.x == 0) {  // commit the per-domain scalars of step n
+            for (int d = 0; d < p.ndom; d++) {
+                if (is_active(ctl, cur, d, p)) {
+                    const double dt = step_dt_at(ctl, ds, cur, d, p, big);
+                    if (!(dt > 1e-9 * p.time_step)) atomicExch(&ctl->error, 2);
+                    const double st = ctl->simtime[cur][d] + dt;
+                    int pid = ctl->pid[cur][d];
+                    if (st >= p.print_interval * (pid + 1)) pid++;
+                    if (p.dtlog) p.dtlog[(size_t)d * p.max_steps + ctl->steps[cur][d]] = dt;
+                    ctl->simtime[1 - cur][d] = st;
+                    ctl->pid[1 - cur][d] = pid;
+                    ctl->steps[1 - cur][d] = ctl->steps[cur][d] + 1;
+                } else {
+                    ctl->simtime[1 - cur][d] = ctl->simtime[cur][d];
+                    ctl->pid[1 - cur][d] = ctl->pid[cur][d];
+                    ctl->steps[1 - cur][d] = ctl->steps[cur][d];
+                }
+                ctl->dtbits[(n + 2) % 3][d] = (unsigned long long)__double_as_longlong(big);
+            }
+        }
+        if (!grid_barrier(ctl, p.spin_limit)) return;
+        if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ticketb[cur] = 0;  // next used two steps later, past a barrier
+    }
+}
+
 static __global__ void flood_init_ctl(Ctl* ctl, int ndom, double big, double t0)
 {
     const int d = threadIdx.x + blockIdx.x * blockDim.x;
@@ -509,6 +719,7 @@ static __global__ void flood_init_ctl(Ctl* ctl, int ndom, double big, double t0)
     }
     if (d < ndom) {
         ctl->src_lo[d] = 0;
+        ctl->dtbits[2][d] = (unsigned long long)__double_as_longlong(big);
         for (int k = 0; k < 2; k++) {
             ctl->dtbits[k][d] = (unsigned long long)__double_as_longlong(big);
             ctl->simtime[k][d] = t0;

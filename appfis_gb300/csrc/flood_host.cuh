@@ -60,8 +60,9 @@ static __global__ void flood_results(const Ctl* __restrict__ ctl, int ndom, int*
         *status = ctl->error == 0 ? APPFIS_GB_OK : (ctl->error == 2 ? APPFIS_GB_ENUMERIC : APPFIS_GB_ETIMEOUT);
 }
 
+// scols: interior columns per strip (SCOLS for the two-phase kernel, FCOLS for the fused one).
 template <class T>
-int make_table(const appfis_gb_flood_domain* doms, int ndom, std::vector<Dom<T>>& tab, long long& total)
+int make_table(const appfis_gb_flood_domain* doms, int ndom, std::vector<Dom<T>>& tab, long long& total, int scols = SCOLS)
 {
     total = 0;
     tab.resize(ndom);
@@ -82,7 +83,7 @@ int make_table(const appfis_gb_flood_domain* doms, int ndom, std::vector<Dom<T>>
         D.nx = s.nx;
         D.ny = s.ny;
         D.px = s.pitch;
-        D.strips_x = (s.nx + SCOLS - 1) / SCOLS;
+        D.strips_x = (s.nx + scols - 1) / scols;
         D.strip0 = total;
         total += (long long)D.strips_x * ((s.ny + ROWS - 1) / ROWS);
     }
@@ -169,9 +170,13 @@ int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_para
     if (!doms || !prm || ndom < 1 || ndom > MAXD) return gb::fail(APPFIS_GB_EINVAL, "flood: 1..%d domains required", MAXD);
     if (!(prm->dx > 0) || !(prm->courant > 0) || !(prm->print_interval > 0) || prm->max_steps < 0)
         return gb::fail(APPFIS_GB_EINVAL, "flood: bad parameters");
+    // the fused pass for the full sweep without point sources
+    bool any_src = false;
+    for (int d = 0; srcs && d < ndom; d++) any_src = any_src || srcs[d].n > 0;
+    const bool fused = !(prm->flags & (APPFIS_GB_FLOOD_SKIP_DRY | APPFIS_GB_FLOOD_TWO_PHASE)) && !any_src;
     std::vector<Dom<T>> tab;
     long long total = 0;
-    GB_TRY(make_table<T>(doms, ndom, tab, total));
+    GB_TRY(make_table<T>(doms, ndom, tab, total, fused ? FCOLS : SCOLS));
     void *wt, *hs;
     GB_TRY(gb::workspace(gb::WS_REDUCE, sizeof(Ctl) + sizeof(Dom<T>) * MAXD + 256, &wt));
     Ctl* ctl = reinterpret_cast<Ctl*>(wt);
@@ -216,7 +221,7 @@ int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_para
 
     int dev = 0, per_sm = 0;
     GB_CUDA(cudaGetDevice(&dev));
-    auto kern = p.zc ? flood_persistent<T, true> : flood_persistent<T, false>;
+    auto kern = fused ? flood_fused<T> : (p.zc ? flood_persistent<T, true> : flood_persistent<T, false>);
     GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
     if (per_sm < 1) return gb::fail(APPFIS_GB_ECUDA, "flood: kernel cannot be resident");
     long long want = (total * 32 + 255) / 256;  // one warp per strip at most

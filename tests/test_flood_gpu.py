@@ -89,3 +89,22 @@ def test_skip_dry_strips_bit_identical(gb, torch_cuda, dtype):
     for k in range(len(doms)):
         assert np.array_equal(full["h"][k], skip["h"][k])
         assert np.array_equal(full["dts"][k], skip["dts"][k])
+
+
+@pytest.mark.parametrize("dtype", [_lib.F32, _lib.F64])
+def test_fused_step_bit_identical_to_two_phase(gb, torch_cuda, dtype):
+    """The fused pass (update, wet/dry fix and next dt in one sweep over 28-column strips whose
+    one-cell ring is recomputed) against the two-pass form: every field, step count and dt
+    identical.  Domains narrower and shorter than one strip, widths on and off the 28- and
+    30-column grids, rows not a multiple of 32, to t_end with the print clamp."""
+    doms = [W.triton_domain(97, 130, 11), W.triton_domain(64, 61, 12), W.triton_domain(150, 40, 13), W.triton_domain(5, 3, 14),
+            W.triton_domain(33, 56, 15), W.triton_domain(40, 29, 16)]
+    args = (10.0, 0.5, 1e-3, 0.035, 300.0, 60.0, 1.0)
+    fused = _lib.flood_job(doms, *args, max_steps=2000, dtype=dtype)
+    two = _lib.flood_job(doms, *args, max_steps=2000, dtype=dtype, flags=_lib.FLOOD_TWO_PHASE)
+    assert fused["steps"] == two["steps"]
+    for k in range(len(doms)):
+        assert np.array_equal(fused["h"][k], two["h"][k]), k
+        assert np.array_equal(fused["qx"][k], two["qx"][k]), k
+        assert np.array_equal(fused["qy"][k], two["qy"][k]), k
+        assert np.array_equal(fused["dts"][k], two["dts"][k]), k
