@@ -44,114 +44,66 @@ __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b)
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 
-// Deterministic block sum of v, then the last block folds all partials into *out.
-__device__ __forceinline__ void gosa_reduce(double v, double* __restrict__ partials, unsigned* __restrict__ ticket,
-                                            double* __restrict__ out)
+// gosa without atomics: each block of a sweep writes the sums of its values to
+// part[vals * block + v]; block 0 of the next launch on the stream, after its own work, folds the
+// previous launch's sums into that launch's gosa values (the previous launch has finished by
+// then), and himeno_gosa_fold folds those of the last launch before a correction pass or the end.
+// Each value is folded in a fixed order (strided per thread, then a shuffle tree, then the warps
+// in order), so gosa is deterministic.
+struct GosaIO {
+    double* part;        // this launch's block sums (null: no gosa)
+    const double* prev;  // the previous launch's block sums (null: nothing to fold)
+    double* prev_out;    // its gosa values
+    unsigned prev_n;     // its block count
+    int prev_vals;       // its sums per block (1, or 2 for a two-sweep pass)
+};
+
+__device__ __forceinline__ double block_sum(double v, double* sh)
 {
-    __shared__ double sh[32];
-    __shared__ bool last;
     const int nthreads = blockDim.x * blockDim.y;
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();  // sh may still be read from an earlier call
     if ((t & 31) == 0) sh[t >> 5] = v;
     __syncthreads();
-    const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
-    const unsigned b = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    if (t < 32) {
-        v = t < (nthreads >> 5) ? sh[t] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (t == 0) {
-            partials[b] = v;
-            __threadfence();
-            last = atomicAdd(ticket, 1u) == nblk - 1;
-        }
-    }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    double w = 0.0;
-    for (unsigned q = t; q < nblk; q += nthreads) w += ((volatile double*)partials)[q];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
-    __syncthreads();
-    if ((t & 31) == 0) sh[t >> 5] = w;
-    __syncthreads();
-    if (t == 0) {
-        double s = 0.0;
+    double s = 0.0;
+    if (t == 0)
         for (int q = 0; q < (nthreads >> 5); q++) s += sh[q];
-        *out = s;
-        *ticket = 0;
+    return s;  // thread 0
+}
+
+__device__ void gosa_fold(const GosaIO& g)
+{
+    __shared__ double sh[32];
+    const int nthreads = blockDim.x * blockDim.y;
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int w = 0; w < g.prev_vals; w++) {
+        double v = 0.0;
+        for (unsigned b = t; b < g.prev_n; b += nthreads) v += g.prev[(size_t)g.prev_vals * b + w];
+        const double s = block_sum(v, sh);
+        if (t == 0) g.prev_out[w] = s;
     }
 }
 
-// gosa_reduce for two sums at once (the two sweeps of one pass): partials[2b], partials[2b+1],
-// folded by the last block into out[0], out[1], each in block order.
-__device__ __forceinline__ void gosa_reduce2(double v1, double v2, double* __restrict__ partials, unsigned* __restrict__ ticket,
-                                             double* __restrict__ out)
+// The end of a sweep kernel: this block's sums of its NV values, then (block 0) the fold of the
+// previous launch.
+template <int NV>
+__device__ __forceinline__ void gosa_end(const double (&v)[NV], const GosaIO& g)
 {
-    __shared__ double sh[2][32];
-    __shared__ bool last;
-    const int nthreads = blockDim.x * blockDim.y;
-    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    __shared__ double sh[32];
+    if (g.part) {
+        const unsigned b = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        v1 += __shfl_down_sync(0xffffffffu, v1, o);
-        v2 += __shfl_down_sync(0xffffffffu, v2, o);
-    }
-    if ((t & 31) == 0) {
-        sh[0][t >> 5] = v1;
-        sh[1][t >> 5] = v2;
-    }
-    __syncthreads();
-    const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
-    const unsigned b = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    if (t < 32) {
-        v1 = t < (nthreads >> 5) ? sh[0][t] : 0.0;
-        v2 = t < (nthreads >> 5) ? sh[1][t] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            v1 += __shfl_down_sync(0xffffffffu, v1, o);
-            v2 += __shfl_down_sync(0xffffffffu, v2, o);
-        }
-        if (t == 0) {
-            partials[2 * b] = v1;
-            partials[2 * b + 1] = v2;
-            __threadfence();
-            last = atomicAdd(ticket, 1u) == nblk - 1;
+        for (int w = 0; w < NV; w++) {
+            const double s = block_sum(v[w], sh);
+            if (threadIdx.x == 0 && threadIdx.y == 0) g.part[(size_t)NV * b + w] = s;
         }
     }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    double w1 = 0.0, w2 = 0.0;
-    for (unsigned q = t; q < nblk; q += nthreads) {
-        w1 += ((volatile double*)partials)[2 * q];
-        w2 += ((volatile double*)partials)[2 * q + 1];
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        w1 += __shfl_down_sync(0xffffffffu, w1, o);
-        w2 += __shfl_down_sync(0xffffffffu, w2, o);
-    }
-    __syncthreads();
-    if ((t & 31) == 0) {
-        sh[0][t >> 5] = w1;
-        sh[1][t >> 5] = w2;
-    }
-    __syncthreads();
-    if (t == 0) {
-        double s1 = 0.0, s2 = 0.0;
-        for (int q = 0; q < (nthreads >> 5); q++) {
-            s1 += sh[0][q];
-            s2 += sh[1][q];
-        }
-        out[0] = s1;
-        out[1] = s2;
-        *ticket = 0;
-    }
+    if (g.prev && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) gosa_fold(g);
 }
+
+__global__ void himeno_gosa_fold(GosaIO g) { gosa_fold(g); }
 
 // Per-thread sum of squares in two floats (hi + lo, ~48 significant bits): the square is split
 // exactly with an FMA and added with an exact two-sum, so a thread's few dozen terms stay within
@@ -202,16 +154,17 @@ __global__ void himeno_half_coef(Coef12 cf, __half* __restrict__ w, size_t field
 template <int BX, int BY>
 __global__ void __launch_bounds__(BX* BY) himeno_correct(Coef12 cf, const float* __restrict__ P, const __half* __restrict__ e,
                                                           float* __restrict__ Pn, __half* __restrict__ D,
-                                                          __half* __restrict__ ezero, int nx, int ny, int nz, int px,
-                                                          int py, int kz, float omega)
+                                                          __half* __restrict__ enext, int nx, int ny, int nz, int px,
+                                                          int py, int kz, float omega, float inv_omega, int prime, GosaIO gz)
 {
     const int i = 1 + blockIdx.x * BX + threadIdx.x;
     const int j = 1 + blockIdx.y * BY + threadIdx.y;
     const int k0 = 1 + blockIdx.z * kz, k1 = min(k0 + kz, nz + 1);
-    if (i > nx || j > ny) return;
+    const bool act = i <= nx && j <= ny;
     const ptrdiff_t plane = (ptrdiff_t)px * py;
     ptrdiff_t c = ((ptrdiff_t)k0 * py + j) * px + i;
-    for (int k = k0; k < k1; k++) {
+    float g = 0.0f;
+    for (int k = k0; act && k < k1; k++) {
 #define QF(di, dj, dk)                                                                                      \
     (__ldg(P + c + (ptrdiff_t)(di) + (ptrdiff_t)(dj) * px + (ptrdiff_t)(dk) * (ptrdiff_t)plane) +          \
      __half2float(e[c + (ptrdiff_t)(di) + (ptrdiff_t)(dj) * px + (ptrdiff_t)(dk) * (ptrdiff_t)plane]))
@@ -221,11 +174,17 @@ __global__ void __launch_bounds__(BX* BY) himeno_correct(Coef12 cf, const float*
                                    __ldg(cf.c[9] + c), __ldg(cf.c[11] + c));
 #undef QF
         const float ss = (s0 * __ldg(cf.c[3] + c) - q0) * __ldg(cf.c[10] + c);
+        const __half dh = __float2half_rn(omega * ss);
         Pn[c] = q0;
-        D[c] = __float2half_rn(omega * ss);
-        ezero[c] = __float2half_rn(0.0f);
+        D[c] = dh;
+        enext[c] = prime ? dh : __float2half_rn(0.0f);
+        if (prime) {  // the next sweep from e = 0 gives e = D exactly, with ss = D / omega
+            const float s1 = __half2float(dh) * inv_omega;
+            g = __fmaf_rn(s1, s1, g);
+        }
         c += plane;
     }
+    gosa_end<1>({(double)g}, gz);
 }
 
 // ---------------------------------------------------------------- 2.5-D forms with a shared plane ring
@@ -278,8 +237,7 @@ __device__ __forceinline__ void ring_store(float* slot, int t, int tx, int ty, i
 template <int MODE>  // 0: plain FP32 sweep of p; 1: FP16 correction sweep of e
 __global__ void __launch_bounds__(RX* RY) himeno_ring(Coef12 cf, H10 hf, const void* __restrict__ pin, void* __restrict__ pout,
                                                        const __half* __restrict__ D, int nx, int ny, int nz, int px, int py,
-                                                       int kz, float omega, float inv_omega, double* __restrict__ partials,
-                                                       unsigned* __restrict__ ticket, double* __restrict__ gosa)
+                                                       int kz, float omega, float inv_omega, GosaIO gz)
 {
     __shared__ float ring[4][RSLOT];
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * RX + tx;
@@ -375,7 +333,7 @@ __global__ void __launch_bounds__(RX* RY) himeno_ring(Coef12 cf, H10 hf, const v
         }
         __syncthreads();
     }
-    if (gosa) gosa_reduce(g.value(), partials, ticket, gosa);
+    gosa_end<1>({g.value()}, gz);
 }
 
 // ---------------------------------------------------------------- TMA-staged FP32 sweep
@@ -403,8 +361,7 @@ struct TmaLayout {
 template <int S>
 __global__ void __launch_bounds__(RX* RY) himeno_tma(const __grid_constant__ TileMaps maps, float* __restrict__ pout, int nx, int ny,
                                                       int nz, int pitch, int py, int kz, float omega,
-                                                      double* __restrict__ partials, unsigned* __restrict__ ticket,
-                                                      double* __restrict__ gosa, unsigned* __restrict__ status)
+                                                      GosaIO gz, unsigned* __restrict__ status)
 {
     typedef TmaLayout Lay;
     typedef float L;
@@ -421,7 +378,7 @@ __global__ void __launch_bounds__(RX* RY) himeno_tma(const __grid_constant__ Til
     const bool act = i >= 1 && i <= nx && j <= ny;
     if (gb::tma::smem_u32(tsm) & 127u) {  // uniform: the copies need 128-byte aligned destinations
         if (t == 0) atomicOr(status, (unsigned)gb::ST_SMEM_ALIGN);
-        if (gosa) gosa_reduce(__longlong_as_double(0x7ff8000000000000ll), partials, ticket, gosa);
+        gosa_end<1>({__longlong_as_double(0x7ff8000000000000ll)}, gz);
         return;
     }
     if (t == 0) {
@@ -486,7 +443,7 @@ __global__ void __launch_bounds__(RX* RY) himeno_tma(const __grid_constant__ Til
                 gb::tma::wait(&bar[(kk - k0) % S], (unsigned)((kk - k0) / S) & 1u, gb::tma::DRAIN_NS);
         }
     }
-    if (gosa) gosa_reduce(k < k1 ? __longlong_as_double(0x7ff8000000000000ll) : g.value(), partials, ticket, gosa);
+    gosa_end<1>({k < k1 ? __longlong_as_double(0x7ff8000000000000ll) : g.value()}, gz);
 }
 
 // ---------------------------------------------------------------- FP16 inner sweep, two points per thread
@@ -587,9 +544,7 @@ __device__ __forceinline__ void mix_pair(const PlaneSet& m, const PlaneSet& z, f
 template <int S, int TW>
 __global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_constant__ TileMaps maps, __half* __restrict__ eout,
                                                              int nx, int ny, int nz, int pitch, int py, int kz, float omega,
-                                                             float inv_omega, double* __restrict__ partials,
-                                                             unsigned* __restrict__ ticket, double* __restrict__ gosa,
-                                                             unsigned* __restrict__ status)
+                                                             float inv_omega, GosaIO gz, unsigned* __restrict__ status)
 {
     namespace f2 = gb::f2;
     typedef MixTile<TW> L;
@@ -609,7 +564,7 @@ __global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_consta
     const bool acta = xa >= 1 && xa <= nx && j <= ny, actb = xa + 1 <= nx && j <= ny;
     if (gb::tma::smem_u32(tsm) & 127u) {
         if (t == 0) atomicOr(status, (unsigned)gb::ST_SMEM_ALIGN);
-        if (gosa) gosa_reduce(__longlong_as_double(0x7ff8000000000000ll), partials, ticket, gosa);
+        gosa_end<1>({__longlong_as_double(0x7ff8000000000000ll)}, gz);
         return;
     }
     if (t == issuer) {
@@ -687,7 +642,7 @@ __global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_consta
         for (int kk = k; kk < min(k + S, k1); kk++)
                 gb::tma::wait(&bar[(kk - k0) % S], (unsigned)((kk - k0) / S) & 1u, gb::tma::DRAIN_NS);
     }
-    if (gosa) gosa_reduce(k < k1 ? __longlong_as_double(0x7ff8000000000000ll) : (double)g.x + (double)g.y, partials, ticket, gosa);
+    gosa_end<1>({k < k1 ? __longlong_as_double(0x7ff8000000000000ll) : (double)g.x + (double)g.y}, gz);
 }
 
 // ---------------------------------------------------------------- FP16 inner sweeps, two per pass
@@ -727,8 +682,7 @@ __device__ __forceinline__ void e_box72_to_f32(const unsigned char* src, float* 
 
 __global__ void __launch_bounds__(T2NT, 2) himeno_mixed_tb2(const __grid_constant__ TileMaps maps, __half* __restrict__ eout, int nx,
                                                             int ny, int nz, int pitch, int py, int kz, float omega, float inv_omega,
-                                                            double* __restrict__ partials, unsigned* __restrict__ ticket,
-                                                            double* __restrict__ gosa, unsigned* __restrict__ status)
+                                                            GosaIO gz, unsigned* __restrict__ status)
 {
     namespace f2 = gb::f2;
     extern __shared__ __align__(128) unsigned char tsm[];
@@ -744,7 +698,7 @@ __global__ void __launch_bounds__(T2NT, 2) himeno_mixed_tb2(const __grid_constan
     const double nan = __longlong_as_double(0x7ff8000000000000ll);
     if (gb::tma::smem_u32(tsm) & 127u) {
         if (t == 0) atomicOr(status, (unsigned)gb::ST_SMEM_ALIGN);
-        if (gosa) gosa_reduce2(nan, nan, partials, ticket, gosa);
+        gosa_end<2>({nan, nan}, gz);
         return;
     }
     if (t == issuer) {
@@ -858,10 +812,8 @@ __global__ void __launch_bounds__(T2NT, 2) himeno_mixed_tb2(const __grid_constan
         atomicOr(status, (unsigned)gb::ST_TMA_TIMEOUT);
         for (int j = i; j <= last_issued; j++) gb::tma::wait(&bar[j % T2S], (unsigned)(j / T2S) & 1u, gb::tma::DRAIN_NS);
     }
-    if (gosa) {
-        const bool ok = i == nst;
-        gosa_reduce2(ok ? (double)g1.x + (double)g1.y : nan, ok ? (double)g2.x + (double)g2.y : nan, partials, ticket, gosa);
-    }
+    const bool ok = i == nst;
+    gosa_end<2>({ok ? (double)g1.x + (double)g1.y : nan, ok ? (double)g2.x + (double)g2.y : nan}, gz);
 }
 
 // ---------------------------------------------------------------- TMA-staged correction pass
@@ -893,9 +845,9 @@ __device__ __forceinline__ void q_box(const unsigned char* pbox, const unsigned 
 
 template <int S>
 __global__ void __launch_bounds__(RX* RY) himeno_correct_tma(const __grid_constant__ CorrMaps maps, float* __restrict__ Pn,
-                                                              __half* __restrict__ D, __half* __restrict__ ezero, int nx, int ny,
-                                                              int nz, int pitch, int py, int kz, float omega,
-                                                              unsigned* __restrict__ status)
+                                                              __half* __restrict__ D, __half* __restrict__ enext, int nx, int ny,
+                                                              int nz, int pitch, int py, int kz, float omega, float inv_omega,
+                                                              int prime, GosaIO gz, unsigned* __restrict__ status)
 {
     typedef TmaLayout Lay;
     extern __shared__ __align__(128) unsigned char tsm[];
@@ -910,6 +862,7 @@ __global__ void __launch_bounds__(RX* RY) himeno_correct_tma(const __grid_consta
     const bool act = i >= 1 && i <= nx && j <= ny;
     if (gb::tma::smem_u32(tsm) & 127u) {
         if (t == 0) atomicOr(status, (unsigned)gb::ST_SMEM_ALIGN);
+        gosa_end<1>({__longlong_as_double(0x7ff8000000000000ll)}, gz);
         return;
     }
     if (t == 0) {
@@ -940,6 +893,7 @@ __global__ void __launch_bounds__(RX* RY) himeno_correct_tma(const __grid_consta
 
     bool bad = false;
     int k = k0;
+    float g = 0.0f;
     const int cq = ty * RX + tx;
     const int q = (ty + 1) * Lay::W + tx + Lay::XO;
     for (; k < k1; k++) {
@@ -964,9 +918,14 @@ __global__ void __launch_bounds__(RX* RY) himeno_correct_tma(const __grid_consta
 #undef RF
             const float ss = (s0v * co[3] - q0) * co[10];
             const size_t cc = ((size_t)k * py + j) * pitch + i;
+            const __half dh = __float2half_rn(omega * ss);
             Pn[cc] = q0;
-            D[cc] = __float2half_rn(omega * ss);
-            ezero[cc] = __float2half_rn(0.0f);
+            D[cc] = dh;
+            enext[cc] = prime ? dh : __float2half_rn(0.0f);
+            if (prime) {  // the next sweep from e = 0 gives e = D exactly, with ss = D / omega
+                const float s1 = __half2float(dh) * inv_omega;
+                g = __fmaf_rn(s1, s1, g);
+            }
         }
         // everyone is done with stage s, the slot of plane k-1 and the sums of plane k+2
         if (__syncthreads_or(bad)) break;
@@ -977,6 +936,7 @@ __global__ void __launch_bounds__(RX* RY) himeno_correct_tma(const __grid_consta
         for (int kk = k; kk < min(k + S, k1); kk++)
             gb::tma::wait(&bar[(kk - k0) % S], (unsigned)((kk - k0) / S) & 1u, gb::tma::DRAIN_NS);
     }
+    gosa_end<1>({k < k1 ? __longlong_as_double(0x7ff8000000000000ll) : (double)g}, gz);
 }
 
 // HKZ: z planes per CTA (nz is split into equal chunks of at most HKZ planes)
@@ -1008,16 +968,48 @@ int check_dims(int nx, int ny, int nz, int pitch)
     return APPFIS_GB_OK;
 }
 
-int gosa_scratch(dim3 grd, double** partials, unsigned** ticket, cudaStream_t st)
-{
-    void* ws;
-    const size_t nblk = (size_t)grd.x * grd.y * grd.z;
-    GB_TRY(gb::workspace(gb::WS_REDUCE, 256 + sizeof(double) * nblk, &ws));
-    *ticket = reinterpret_cast<unsigned*>(ws);
-    *partials = reinterpret_cast<double*>(reinterpret_cast<char*>(ws) + 256);
-    GB_CUDA(cudaMemsetAsync(*ticket, 0, sizeof(unsigned), st));
-    return APPFIS_GB_OK;
-}
+// The gosa block sums of a sequence of sweep launches (two buffers, used in turn) and the fold
+// still owed for the last launch.
+struct GosaSeq {
+    double* buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    GosaIO pend = {};
+    // the scratch for launches of at most `blocks` blocks of `vals` sums each (no-op without gosa)
+    int init(bool on, size_t blocks, int vals)
+    {
+        if (!on) return APPFIS_GB_OK;
+        void* ws;
+        const size_t n = blocks * (size_t)vals;
+        GB_TRY(gb::workspace(gb::WS_REDUCE, 2 * sizeof(double) * n, &ws));
+        buf[0] = reinterpret_cast<double*>(ws);
+        buf[1] = buf[0] + n;
+        return APPFIS_GB_OK;
+    }
+    // the GosaIO of the next launch (grid grd, `vals` sums per block, gosa values at out; out
+    // null: no gosa), which folds the previous launch's sums
+    GosaIO next(dim3 grd, int vals, double* out)
+    {
+        GosaIO g = {nullptr, pend.prev, pend.prev_out, pend.prev_n, pend.prev_vals};
+        pend = {};
+        if (out && buf[0]) {
+            g.part = buf[cur];
+            pend.prev = buf[cur];
+            pend.prev_out = out;
+            pend.prev_n = grd.x * grd.y * grd.z;
+            pend.prev_vals = vals;
+            cur ^= 1;
+        }
+        return g;
+    }
+    // folds what is owed (before a launch that takes no GosaIO, and at the end)
+    int flush(cudaStream_t st)
+    {
+        if (!pend.prev) return APPFIS_GB_OK;
+        himeno_gosa_fold<<<1, 256, 0, st>>>(pend);
+        pend = {};
+        return gb::launched("himeno_gosa_fold");
+    }
+};
 
 }  // namespace
 
@@ -1035,8 +1027,7 @@ int appfis_gb_himeno(const float* const* coef, float* p, float* wrk2, int nx, in
     Coef12 cf;
     for (int n = 0; n < 12; n++) cf.c[n] = coef[n];
     dim3 blk(RX, RY), grd(gb::ceil_div(nx, RX), gb::ceil_div(ny, RY), gb::ceil_div(nz, HKZ));
-    double* partials = nullptr;
-    unsigned* ticket = nullptr;
+    GosaSeq gs;
     float* buf[2] = {p, wrk2};
     int ci = 0;
     if (plain_tma_ok(coef, p, wrk2, pitch)) {
@@ -1050,26 +1041,28 @@ int appfis_gb_himeno(const float* const* coef, float* p, float* wrk2, int nx, in
         GB_TRY(gb::status_word(&status));
         const int kz = gb::balanced_chunk(nz, HKZ);
         dim3 tgrd(nx / RX + 1, gb::ceil_div(ny, RY), gb::ceil_div(nz, kz));
-        if (dev_gosa) GB_TRY(gosa_scratch(tgrd, &partials, &ticket, st));
+        GB_TRY(gs.init(dev_gosa, (size_t)tgrd.x * tgrd.y * tgrd.z, 1));
         constexpr int smem = TmaLayout::smem(TMA_S_PLAIN);
         GB_CUDA(cudaFuncSetAttribute(himeno_tma<TMA_S_PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         for (int it = 0; it < iters; it++) {
-            himeno_tma<TMA_S_PLAIN><<<tgrd, blk, smem, st>>>(maps[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2, kz, omega, partials,
-                                                            ticket, dev_gosa ? dev_gosa + it : nullptr, status);
+            himeno_tma<TMA_S_PLAIN><<<tgrd, blk, smem, st>>>(maps[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2, kz, omega,
+                                                            gs.next(tgrd, 1, dev_gosa ? dev_gosa + it : nullptr), status);
             ci = 1 - ci;
         }
         GB_TRY(gb::launched("himeno_tma<plain>"));
+        GB_TRY(gs.flush(st));
         if (cur_index) *cur_index = ci;
         return APPFIS_GB_OK;
     }
-    if (dev_gosa) GB_TRY(gosa_scratch(grd, &partials, &ticket, st));
+    GB_TRY(gs.init(dev_gosa, (size_t)grd.x * grd.y * grd.z, 1));
     H10 none = {};
     for (int it = 0; it < iters; it++) {
         himeno_ring<0><<<grd, blk, 0, st>>>(cf, none, buf[ci], buf[1 - ci], nullptr, nx, ny, nz, pitch, ny + 2, HKZ, omega, 0.0f,
-                                            partials, ticket, dev_gosa ? dev_gosa + it : nullptr);
+                                            gs.next(grd, 1, dev_gosa ? dev_gosa + it : nullptr));
         ci = 1 - ci;
     }
     GB_TRY(gb::launched("himeno_ring<plain>"));
+    GB_TRY(gs.flush(st));
     if (cur_index) *cur_index = ci;
     return APPFIS_GB_OK;
 }
@@ -1174,17 +1167,17 @@ int appfis_gb_himeno_mixed_ex(const float* const* coef, float* p, float* p_work,
         t2kz = gb::wave_chunk(nz, 32, 64, (long long)t2x * t2y, (long long)per_sm * gb::sm_count(), 2);
         t2grd = dim3(t2x, t2y, gb::ceil_div(nz, t2kz));
     }
-    double* rpartials = nullptr;
-    unsigned* rticket = nullptr;
-    if (dev_gosa) {
-        const unsigned nb1 = use_tma ? tgrd.x * tgrd.y * tgrd.z : rgrd.x * rgrd.y * rgrd.z;
-        const unsigned nb2 = two ? 2 * t2grd.x * t2grd.y * t2grd.z : 0;
-        GB_TRY(gosa_scratch(dim3(std::max(nb1, nb2)), &rpartials, &rticket, st));
-    }
     float* P[2] = {p, p_work};
     // correction maps: [P buffer][e buffer]
     CorrMaps cmaps[2][2];
     dim3 cgrd(nx / RX + 1, gb::ceil_div(ny, RY), gb::ceil_div(nz, tkz));
+    GosaSeq gs;  // block sums of the sweeps and of the correction passes (which do a sweep each)
+    {
+        const unsigned nb1 = use_tma ? tgrd.x * tgrd.y * tgrd.z : rgrd.x * rgrd.y * rgrd.z;
+        const unsigned nb2 = two ? 2 * t2grd.x * t2grd.y * t2grd.z : 0;
+        const unsigned nb3 = use_tma ? cgrd.x * cgrd.y * cgrd.z : grd.x * grd.y * grd.z;
+        GB_TRY(gs.init(dev_gosa, std::max(std::max(nb1, nb2), nb3), 1));
+    }
     constexpr int csmem = corr_smem(CORR_S);
     if (use_tma) {
         const int py = ny + 2;
@@ -1201,37 +1194,47 @@ int appfis_gb_himeno_mixed_ex(const float* const* coef, float* p, float* p_work,
         GB_CUDA(cudaFuncSetAttribute(himeno_correct_tma<CORR_S>, cudaFuncAttributeMaxDynamicSharedMemorySize, csmem));
     }
     int pc = 0, ec = 0;
-    // the correction pass: P' = P + e into the other P buffer, D, the other e buffer zeroed
-    auto correct = [&]() {
+    const float inv_omega = 1.0f / omega;
+    // The correction pass: P' = P + e into the other P buffer and D; with `prime` it also does
+    // the next period's first inner sweep, which from e = 0 yields e = D exactly (all neighbour
+    // terms vanish), so it writes e = D and that sweep's gosa; otherwise e = 0.
+    auto correct = [&](bool prime, double* g) {
+        const GosaIO gz = gs.next(use_tma ? cgrd : grd, 1, prime ? g : nullptr);
         if (use_tma)
             himeno_correct_tma<CORR_S><<<cgrd, rblk, csmem, st>>>(cmaps[pc][ec], P[1 - pc], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2,
-                                                                 tkz, omega, status);
+                                                                 tkz, omega, inv_omega, prime ? 1 : 0, gz, status);
         else
             himeno_correct<HBX, HBY><<<grd, blk, 0, st>>>(cf, P[pc], E[ec], P[1 - pc], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2,
-                                                          HKZ, omega);
+                                                          HKZ, omega, inv_omega, prime ? 1 : 0, gz);
         pc = 1 - pc;
         ec = 1 - ec;
     };
-    correct();  // D from the initial P (e = 0), e restarted at 0
-    const float inv_omega = 1.0f / omega;
-    for (int it = 0; it < iters;) {
-        const int left = std::min(iters - it, period - it % period);  // sweeps before the next correction
-        if (two && left >= 2) {
-            himeno_mixed_tb2<<<t2grd, T2NT, t2_smem(), st>>>(t2maps[ec], E[1 - ec], nx, ny, nz, pitch, ny + 2, t2kz, omega, inv_omega,
-                                                           rpartials, rticket, dev_gosa ? dev_gosa + it : nullptr, status);
-            it += 2;
-        } else {
-            if (use_tma)
-                tkern<<<tgrd, tblk, tsmem, st>>>(tmaps[ec], E[1 - ec], nx, ny, nz, pitch, ny + 2, tkz, omega, inv_omega, rpartials,
-                                                 rticket, dev_gosa ? dev_gosa + it : nullptr, status);
-            else
-                himeno_ring<1><<<rgrd, rblk, 0, st>>>(cf, hf, E[ec], E[1 - ec], Dd, nx, ny, nz, pitch, ny + 2, HKZ, omega, inv_omega,
-                                                      rpartials, rticket, dev_gosa ? dev_gosa + it : nullptr);
-            it += 1;
+    // periods of `period` sweeps, each opened by a correction pass that does its first sweep;
+    // the last correction closes the run
+    for (int it = 0;;) {
+        const bool prime = it < iters;
+        correct(prime, dev_gosa ? dev_gosa + it : nullptr);
+        if (!prime) break;
+        const int end = std::min(iters, it + period);
+        it += 1;
+        while (it < end) {
+            if (two && end - it >= 2) {
+                himeno_mixed_tb2<<<t2grd, T2NT, t2_smem(), st>>>(t2maps[ec], E[1 - ec], nx, ny, nz, pitch, ny + 2, t2kz, omega, inv_omega,
+                                                               gs.next(t2grd, 2, dev_gosa ? dev_gosa + it : nullptr), status);
+                it += 2;
+            } else {
+                if (use_tma)
+                    tkern<<<tgrd, tblk, tsmem, st>>>(tmaps[ec], E[1 - ec], nx, ny, nz, pitch, ny + 2, tkz, omega, inv_omega,
+                                                     gs.next(tgrd, 1, dev_gosa ? dev_gosa + it : nullptr), status);
+                else
+                    himeno_ring<1><<<rgrd, rblk, 0, st>>>(cf, hf, E[ec], E[1 - ec], Dd, nx, ny, nz, pitch, ny + 2, HKZ, omega,
+                                                          inv_omega, gs.next(rgrd, 1, dev_gosa ? dev_gosa + it : nullptr));
+                it += 1;
+            }
+            ec = 1 - ec;
         }
-        ec = 1 - ec;
-        if (it % period == 0 || it == iters) correct();
     }
+    GB_TRY(gs.flush(st));
     GB_TRY(gb::launched("himeno_mixed"));
     if (cur_index) *cur_index = pc;
     return APPFIS_GB_OK;

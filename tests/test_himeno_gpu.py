@@ -188,3 +188,26 @@ def test_mixed_two_sweeps_needs_aligned_rows(gb, torch_cuda):
     nx, ny, nz = 13, 5, 4
     with pytest.raises(_lib.AppfisError):
         device_run(gb, torch_cuda, W.himeno_coef(nx, ny, nz), W.himeno_p(nx, ny, nz), 2, nx + 2, form=1, spp=2)
+
+
+@pytest.mark.parametrize("iters,period", [(1, 20), (2, 1), (3, 2), (5, 2), (7, 3)])
+@pytest.mark.parametrize("spp", [1, 2])
+def test_mixed_short_runs_and_periods(gb, torch_cuda, iters, period, spp):
+    """Each correction pass also does its period's first inner sweep (from e = 0 it gives e = D);
+    short runs and short periods (every sweep such a first one at period 1) against the FP64
+    oracle: p within the mixed form's 2.5e-4, gosa of every sweep within 1%."""
+    nx, ny, nz = 40, 13, 11
+    pitch = (nx + 2 + 7) // 8 * 8
+    p64, g64 = O.himeno(W.himeno_coef(nx, ny, nz, dtype=np.float64), W.himeno_p(nx, ny, nz, dtype=np.float64), iters, 0.8,
+                        dtype=np.float64)
+    mixed, gm = device_run(gb, torch_cuda, W.himeno_coef(nx, ny, nz), W.himeno_p(nx, ny, nz), iters, pitch, form=1, period=period,
+                           spp=spp)
+    assert np.abs(mixed - p64).max() < 2.5e-4
+    np.testing.assert_allclose(gm, g64, rtol=1e-2)
+
+
+def test_mixed_zero_sweeps_leaves_p(gb, torch_cuda):
+    nx, ny, nz = 30, 9, 7
+    p = W.himeno_p(nx, ny, nz)
+    out, _ = device_run(gb, torch_cuda, W.himeno_coef(nx, ny, nz), p, 0, 32, form=1)
+    assert np.array_equal(out, p)
