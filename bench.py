@@ -944,6 +944,18 @@ def profile_small(name, torch, gb, W, dev, sp):
                 ctypes.byref(ci), sp.cuda_stream)
         gb.call("appfis_gb_himeno_mixed", ptrs, pa.data_ptr(), pb.data_ptr(), half.data_ptr(), nx, ny, nz, pitch, 5, 20,
                 c["omega"], gosa.data_ptr(), ctypes.byref(ci), sp.cuda_stream)
+    elif name == "himeno-small":
+        nx, ny, nz = 129, 129, 257
+        pitch = (nx + 2 + 7) // 8 * 8
+        coef = _pad_x(torch.from_numpy(W.himeno_coef(nx, ny, nz)).to(dev), pitch)
+        p0 = _pad_x(torch.from_numpy(W.himeno_p(nx, ny, nz)).to(dev), pitch)
+        ptrs = (ctypes.c_void_p * 12)(*[coef[k].data_ptr() for k in range(12)])
+        pa, pb = p0.clone(), p0.clone()
+        half = torch.empty(13 * p0.numel(), dtype=torch.float16, device=dev)
+        gosa = torch.zeros(8, dtype=torch.float64, device=dev)
+        for spp in (1, 2):  # 1 + 2 inner sweeps: himeno_mixed2, then himeno_mixed_tb2
+            gb.call("appfis_gb_himeno_mixed_ex", ptrs, pa.data_ptr(), pb.data_ptr(), half.data_ptr(), nx, ny, nz, pitch, 4, 1000,
+                    0.8, spp, gosa.data_ptr(), ctypes.byref(ci), sp.cuda_stream)
     elif name == "fdtd":
         c = W.FDTD
         nx, ny, nz = c["nx"], c["ny"], c["nz"]
@@ -971,7 +983,10 @@ def profile_case(name, local):
     fdtd:   512^3, 5 FP32 steps then 5 FP16 steps (star_r4_tma), then 2 two-step launches in FP32
             and 2 in FP16 (star_r4_tb2)
     heat:   1024^2, 16 iterations (2 heat2d_regs launches)
-    flood:  the 32-domain batch (80 M cells, ~2.6 GB), 20 steps (one flood_persistent launch)"""
+    himeno-small: 129x129x257, the mixed form with one inner sweep per launch (himeno_mixed2),
+            then with two (himeno_mixed_tb2), 4 sweeps each (~0.3 GB)
+    flood:  the 32-domain batch (80 M cells, ~2.6 GB), 20 steps (one flood_fused launch)
+    flood-small: the first 6 domains of the batch (15.8 M cells), 20 steps (one flood_fused launch)"""
     import torch
 
     import appfis_gb300 as gb
@@ -981,10 +996,12 @@ def profile_case(name, local):
     sp = torch.cuda.current_stream(dev)
     if name != "life":
         fn = {"himeno": bench_himeno, "fdtd": bench_fdtd, "heat": bench_heat}.get(name)
-        if name == "flood":
+        if name in ("flood", "flood-small"):
             from appfis_gb300 import _lib
             c = W.TRITON
             doms = W.triton_batch(c["n_domains"], c["side_lo"], c["side_hi"], c["seed"])
+            if name == "flood-small":
+                doms = doms[:6]
             _lib.flood_job(doms, c["dx"], c["courant"], c["hextra"], c["manning"], c["t_end"], c["t_end"], c["time_step"],
                            max_steps=20, dtype=_lib.F32)
         else:
@@ -1018,7 +1035,7 @@ def main():
     ap.add_argument("--apps", default="heat2d,himeno,fdtd3d,flood", help="comma-separated per-workload measurements")
     ap.add_argument("--apps-unchanged", action="store_true",
                     help="time the reference's sample applications on its CPU path, its GPU path and the drop-in")
-    ap.add_argument("--profile-case", choices=["life", "himeno", "fdtd", "heat", "flood"], default=None,
+    ap.add_argument("--profile-case", choices=["life", "himeno", "himeno-small", "fdtd", "heat", "flood", "flood-small"], default=None,
                     help="launch a short fixed sequence of the named workload's kernels (for ncu), no timing")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
