@@ -518,7 +518,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
 constexpr int FCOLS = 28;
 
 template <class T>
-__device__ void phase_bf(const Dom<T> D, long long local, int b, T dt, const Params& p, unsigned long long* dt_next)
+__device__ bool phase_bf(const Dom<T> D, long long local, int b, T dt, const Params& p, unsigned long long* dt_next)
 {
     const int lane = threadIdx.x & 31;
     const int loc = (int)local, sy = loc / D.strips_x, sx = loc - sy * D.strips_x;  // 32-bit: a domain has < 2^31 strips
@@ -558,6 +558,7 @@ __device__ void phase_bf(const Dom<T> D, long long local, int b, T dt, const Par
     T h2 = zero, z2 = zero;                         // row r-2: updated depth, bed
     T h1 = zero, qx1 = zero, qy1 = zero, z1 = zero;  // row r-1: updated state, bed
     T mn = K<T>::big();
+    bool dry = true;  // every cell this lane owns ends with h = qx = qy = 0
     for (int r = ra; r <= rb; r++) {
         const Raw<T> rnn = r + 2 <= rb + 1 ? raw(r + 2) : zr;  // prefetch
         const bool rin = r >= 1 && r <= ny;
@@ -609,6 +610,7 @@ __device__ void phase_bf(const Dom<T> D, long long local, int b, T dt, const Par
                 ho_[c1] = h1;
                 qxo_[c1] = qxr;
                 qyo_[c1] = qyr;
+                dry = dry && h1 == zero && qxr == zero && qyr == zero;
             }
         }
 #pragma unroll
@@ -629,13 +631,14 @@ __device__ void phase_bf(const Dom<T> D, long long local, int b, T dt, const Par
         mn = other < mn ? other : mn;
     }
     if (lane == 0 && mn < K<T>::big()) atomicMin(dt_next, (unsigned long long)__double_as_longlong((double)mn));
+    return __all_sync(0xffffffffu, dry);
 }
 
 // The fused persistent kernel (full sweep, no point sources): a dt-only pass over the initial
 // state, then one pass and one grid barrier per step.  The per-domain CFL minimum of step n is
 // accumulated in dtbits[n % 3] during step n-1, read at the start of step n, and the slot of
 // step n+2 is reset by block 0 during step n (nobody reads or writes it then).
-template <class T>
+template <class T, bool SKIP>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1) flood_fused(const Dom<T>* __restrict__ gdoms, Ctl* ctl,
                                                                                           Params p)
 {
@@ -680,7 +683,19 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
         for_strips(&ctl->ticketb[cur], warp, nwarps, p.total_strips, lane, [&](long long s) {
             const int d = find_domain(doms, p.ndom, s);
             const int f = dc.flags[d];
-            if (f & 4) phase_bf<T>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p, &ctl->dtbits[dn][d]);
+            if (SKIP) {  // the two-phase kernel's dry-strip rule (strip_idle), on this kernel's strips
+                const unsigned char* zin = p.zc + (size_t)cur * p.total_strips;
+                unsigned char* zout = p.zc + (size_t)(1 - cur) * p.total_strips;
+                const unsigned char z = zin[s];
+                if (!(f & 4) || strip_idle(doms[d], zin, s)) {  // unchanged state, no fix, no dt
+                    if (lane == 0) zout[s] = z;
+                    return;
+                }
+                const bool dry = phase_bf<T>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p, &ctl->dtbits[dn][d]);
+                if (lane == 0) zout[s] = dry ? (unsigned char)(z < 2 ? z + 1 : 2) : 0;
+            } else if (f & 4) {
+                phase_bf<T>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p, &ctl->dtbits[dn][d]);
+            }
         });
         if (blockIdx.x == 0 && threadIdx.x == 0) {  // commit the per-domain scalars of step n
             for (int d = 0; d < p.ndom; d++) {

@@ -173,7 +173,7 @@ int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_para
     // the fused pass for the full sweep without point sources
     bool any_src = false;
     for (int d = 0; srcs && d < ndom; d++) any_src = any_src || srcs[d].n > 0;
-    const bool fused = !(prm->flags & (APPFIS_GB_FLOOD_SKIP_DRY | APPFIS_GB_FLOOD_TWO_PHASE)) && !any_src;
+    const bool fused = !(prm->flags & APPFIS_GB_FLOOD_TWO_PHASE) && !any_src;
     std::vector<Dom<T>> tab;
     long long total = 0;
     GB_TRY(make_table<T>(doms, ndom, tab, total, fused ? FCOLS : SCOLS));
@@ -221,7 +221,8 @@ int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_para
 
     int dev = 0, per_sm = 0;
     GB_CUDA(cudaGetDevice(&dev));
-    auto kern = fused ? flood_fused<T> : (p.zc ? flood_persistent<T, true> : flood_persistent<T, false>);
+    auto kern = fused ? (p.zc ? flood_fused<T, true> : flood_fused<T, false>)
+                      : (p.zc ? flood_persistent<T, true> : flood_persistent<T, false>);
     GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
     if (per_sm < 1) return gb::fail(APPFIS_GB_ECUDA, "flood: kernel cannot be resident");
     long long want = (total * 32 + 255) / 256;  // one warp per strip at most

@@ -309,16 +309,16 @@ typedef struct {
     int flags;             /* APPFIS_GB_FLOOD_SKIP_DRY, APPFIS_GB_FLOOD_TWO_PHASE or 0 */
 } appfis_gb_flood_params;
 
-/* flags: strips (30 x 32 cells) whose depth and momentum are exactly 0 and whose four neighbour
+/* flags: strips (28 or 30 x 32 cells) whose depth and momentum are exactly 0 and whose four neighbour
  * strips are dry as well are left out of a step: such cells cannot change (no face of theirs
  * has water on either side), so every field is bit-identical to the full sweep.  A strip is
  * skipped only after its output was dry for two consecutive steps (both state buffers hold the
  * dry state). */
 #define APPFIS_GB_FLOOD_SKIP_DRY 1
-/* The full sweep without point sources runs one fused pass per step (update, wet/dry fix and the
- * next step's CFL dt; 28-column strips whose one-cell ring is updated again by its neighbours).
- * This flag selects the two-pass form (fix + dt, then update) that dry-strip skipping and point
- * sources use; the fields, step counts and dt logs of the two forms are identical. */
+/* Runs without point sources take one fused pass per step (update, wet/dry fix and the next
+ * step's CFL dt; 28-column strips whose one-cell ring is updated again by its neighbours), with
+ * or without dry-strip skipping.  This flag selects the two-pass form (fix + dt, then update)
+ * that point sources use; the fields, step counts and dt logs of the two forms are identical. */
 #define APPFIS_GB_FLOOD_TWO_PHASE 2
 
 #define APPFIS_GB_FLOOD_MAX_DOMAINS 64

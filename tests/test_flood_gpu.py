@@ -108,3 +108,18 @@ def test_fused_step_bit_identical_to_two_phase(gb, torch_cuda, dtype):
         assert np.array_equal(fused["qx"][k], two["qx"][k]), k
         assert np.array_equal(fused["qy"][k], two["qy"][k]), k
         assert np.array_equal(fused["dts"][k], two["dts"][k]), k
+
+
+@pytest.mark.parametrize("dtype", [_lib.F32, _lib.F64])
+def test_fused_skip_dry_bit_identical_to_two_phase_skip_dry(gb, torch_cuda, dtype):
+    """Dry-strip skipping in the fused pass (28-column strips) against the two-phase form with the
+    same skipping (30-column strips): fields, steps and dts identical."""
+    doms = [W.triton_domain(97, 130, 11), W.triton_domain(64, 61, 12), W.triton_domain(150, 40, 13)]
+    args = (10.0, 0.5, 1e-3, 0.035, 600.0, 600.0, 1.0)
+    fused = _lib.flood_job(doms, *args, max_steps=150, dtype=dtype, flags=_lib.FLOOD_SKIP_DRY)
+    two = _lib.flood_job(doms, *args, max_steps=150, dtype=dtype, flags=_lib.FLOOD_SKIP_DRY | _lib.FLOOD_TWO_PHASE)
+    assert fused["steps"] == two["steps"]
+    for k in range(len(doms)):
+        assert np.array_equal(fused["h"][k], two["h"][k])
+        assert np.array_equal(fused["qx"][k], two["qx"][k])
+        assert np.array_equal(fused["dts"][k], two["dts"][k])
