@@ -453,8 +453,9 @@ __global__ void __launch_bounds__(RX* RY) himeno_tma(const __grid_constant__ Til
 // instructions.  Tile 64 x 8 points (32 x 8 threads).  Per plane k a pipeline stage brings the
 // eleven FP16/FP32 per-point tiles of plane k (a0 a1 a2 b0 b1 b2 c0 c1 c2 bnd as FP16, a3 as
 // FP32, D as FP16) and the FP16 box of e plane k+2 (80 x 10, x origin = tile x - 8).  The threads
-// convert that box once into an FP32 ring slot (planes k-1 .. k+2 resident), so the 19 neighbour
-// reads of a pair are 19 FP32 shared loads (paired where the pair's columns are contiguous).
+// convert that box once into an FP32 ring slot (planes k .. k+2 resident), and each thread keeps
+// its pair's neighbour sets of planes k-1 and k in registers, so a plane costs a pair 9 FP32
+// shared loads (paired where the pair's columns are contiguous).
 constexpr int MY = 8, MXO = 8;  // tile rows; x halo of the e box
 constexpr int MIX_S = 2;
 
@@ -465,7 +466,8 @@ struct MixTile {
     static constexpr int EB = W * (MY + 2) * 2, ES = (EB + 127) / 128 * 128;
     static constexpr int CT = 10 * X * MY * 2 + X * MY * 4 + X * MY * 2;
     static constexpr int STG = CT + ES, R32 = W * (MY + 2);
-    static constexpr int smem(int S) { return S * STG + 4 * R32 * 4 + 3 * ES + S * 8; }
+    static constexpr int RB = (3 * R32 * 4 + 127) / 128 * 128;  // the 3-slot ring, a 128-byte multiple
+    static constexpr int smem(int S) { return S * STG + RB + 3 * ES + S * 8; }
 };
 
 template <int TW>
@@ -552,7 +554,7 @@ __global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_consta
     extern __shared__ __align__(128) unsigned char tsm[];
     unsigned char* stages = tsm;
     float* ring = reinterpret_cast<float*>(tsm + S * MSTG);
-    unsigned char* pro = tsm + S * MSTG + 4 * MR32 * 4;
+    unsigned char* pro = tsm + S * MSTG + L::RB;  // copy destinations stay 128-byte aligned
     uint64_t* bar = reinterpret_cast<uint64_t*>(pro + 3 * MES);
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * (MX / 2) + tx;
     // the copies are issued by the last warp's first thread: the e box conversion leaves that
@@ -574,7 +576,9 @@ __global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_consta
         for (int n = 0; n < 13; n++) gb::tma::prefetch_map(&maps.m[n]);
     }
     __syncthreads();
-    auto slot = [&](int pl) { return ring + ((pl - (k0 - 1)) & 3) * MR32; };
+    // e planes k-1 .. k+1 in a 3-slot FP32 ring: a step reads plane k+1's set and plane k's
+    // diagonals (plane k-1 is in the register queue), so plane k+2 can take plane k-1's slot
+    auto slot = [&](int pl) { return ring + ((unsigned)(pl - (k0 - 1)) % 3u) * MR32; };
     auto issue = [&](int k) {
         const int s = (k - k0) % S;
         unsigned char* st = stages + s * MSTG;
@@ -606,8 +610,9 @@ __global__ void __launch_bounds__(TW / 2 * MY) himeno_mixed2(const __grid_consta
             __syncthreads();
             pm = plane_set(slot(k0 - 1), q, MW);
             pz = plane_set(slot(k0), q, MW);
+            __syncthreads();  // plane k0-1's slot is read before plane k0+2 takes it
         }
-        e_box_to_f32<TW>(st + MCT, slot(k + 2), t);  // plane k+2 into the slot plane k-2 left
+        e_box_to_f32<TW>(st + MCT, slot(k + 2), t);  // plane k+2 into the slot plane k-1 left
         {
             float2 co[10];
 #pragma unroll
