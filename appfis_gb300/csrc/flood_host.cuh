@@ -171,9 +171,14 @@ int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_para
     if (!(prm->dx > 0) || !(prm->courant > 0) || !(prm->print_interval > 0) || prm->max_steps < 0)
         return gb::fail(APPFIS_GB_EINVAL, "flood: bad parameters");
     // the fused pass for the full sweep without point sources
+    if ((prm->flags & APPFIS_GB_FLOOD_TWO_PHASE) && (prm->flags & APPFIS_GB_FLOOD_FUSED))
+        return gb::fail(APPFIS_GB_EINVAL, "flood: TWO_PHASE and FUSED are exclusive");
     bool any_src = false;
     for (int d = 0; srcs && d < ndom; d++) any_src = any_src || srcs[d].n > 0;
-    const bool fused = !(prm->flags & APPFIS_GB_FLOOD_TWO_PHASE) && !any_src;
+    // the fused pass by default in FP32; in FP64 (one CTA per SM at ~200 registers) the two-phase
+    // form is faster (full sweep 21.2 against 22.9 s on the 32-domain batch)
+    const bool fused = !any_src && !(prm->flags & APPFIS_GB_FLOOD_TWO_PHASE) &&
+                       ((prm->flags & APPFIS_GB_FLOOD_FUSED) || std::is_same<T, float>::value);
     std::vector<Dom<T>> tab;
     long long total = 0;
     GB_TRY(make_table<T>(doms, ndom, tab, total, fused ? FCOLS : SCOLS));

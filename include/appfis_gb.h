@@ -306,7 +306,7 @@ typedef struct {
     double time_step;      /* dt used while no cell is wet */
     double t_start;        /* initial simulated time */
     int max_steps;         /* 0 = no limit; > 0 also enables the dt log */
-    int flags;             /* APPFIS_GB_FLOOD_SKIP_DRY, APPFIS_GB_FLOOD_TWO_PHASE or 0 */
+    int flags;             /* APPFIS_GB_FLOOD_SKIP_DRY | APPFIS_GB_FLOOD_TWO_PHASE or _FUSED, or 0 */
 } appfis_gb_flood_params;
 
 /* flags: strips (28 or 30 x 32 cells) whose depth and momentum are exactly 0 and whose four neighbour
@@ -315,11 +315,13 @@ typedef struct {
  * skipped only after its output was dry for two consecutive steps (both state buffers hold the
  * dry state). */
 #define APPFIS_GB_FLOOD_SKIP_DRY 1
-/* Runs without point sources take one fused pass per step (update, wet/dry fix and the next
- * step's CFL dt; 28-column strips whose one-cell ring is updated again by its neighbours), with
- * or without dry-strip skipping.  This flag selects the two-pass form (fix + dt, then update)
- * that point sources use; the fields, step counts and dt logs of the two forms are identical. */
+/* FP32 runs without point sources take one fused pass per step (update, wet/dry fix and the
+ * next step's CFL dt; 28-column strips whose one-cell ring is updated again by its neighbours),
+ * with or without dry-strip skipping; FP64 runs and runs with point sources take two passes (fix
+ * + dt, then update).  TWO_PHASE and FUSED (no point sources) select a form explicitly; the
+ * fields, step counts and dt logs of the two forms are identical. */
 #define APPFIS_GB_FLOOD_TWO_PHASE 2
+#define APPFIS_GB_FLOOD_FUSED 4
 
 #define APPFIS_GB_FLOOD_MAX_DOMAINS 64
 

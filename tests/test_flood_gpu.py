@@ -100,7 +100,7 @@ def test_fused_step_bit_identical_to_two_phase(gb, torch_cuda, dtype):
     doms = [W.triton_domain(97, 130, 11), W.triton_domain(64, 61, 12), W.triton_domain(150, 40, 13), W.triton_domain(5, 3, 14),
             W.triton_domain(33, 56, 15), W.triton_domain(40, 29, 16)]
     args = (10.0, 0.5, 1e-3, 0.035, 300.0, 60.0, 1.0)
-    fused = _lib.flood_job(doms, *args, max_steps=2000, dtype=dtype)
+    fused = _lib.flood_job(doms, *args, max_steps=2000, dtype=dtype, flags=_lib.FLOOD_FUSED)
     two = _lib.flood_job(doms, *args, max_steps=2000, dtype=dtype, flags=_lib.FLOOD_TWO_PHASE)
     assert fused["steps"] == two["steps"]
     for k in range(len(doms)):
@@ -116,10 +116,17 @@ def test_fused_skip_dry_bit_identical_to_two_phase_skip_dry(gb, torch_cuda, dtyp
     same skipping (30-column strips): fields, steps and dts identical."""
     doms = [W.triton_domain(97, 130, 11), W.triton_domain(64, 61, 12), W.triton_domain(150, 40, 13)]
     args = (10.0, 0.5, 1e-3, 0.035, 600.0, 600.0, 1.0)
-    fused = _lib.flood_job(doms, *args, max_steps=150, dtype=dtype, flags=_lib.FLOOD_SKIP_DRY)
+    fused = _lib.flood_job(doms, *args, max_steps=150, dtype=dtype, flags=_lib.FLOOD_SKIP_DRY | _lib.FLOOD_FUSED)
     two = _lib.flood_job(doms, *args, max_steps=150, dtype=dtype, flags=_lib.FLOOD_SKIP_DRY | _lib.FLOOD_TWO_PHASE)
     assert fused["steps"] == two["steps"]
     for k in range(len(doms)):
         assert np.array_equal(fused["h"][k], two["h"][k])
         assert np.array_equal(fused["qx"][k], two["qx"][k])
         assert np.array_equal(fused["dts"][k], two["dts"][k])
+
+
+def test_fused_and_two_phase_flags_exclusive(gb, torch_cuda):
+    doms = [W.triton_domain(20, 20, 3)]
+    with pytest.raises(_lib.AppfisError):
+        _lib.flood_job(doms, 10.0, 0.5, 1e-3, 0.035, 60.0, 60.0, 1.0, max_steps=5,
+                       flags=_lib.FLOOD_FUSED | _lib.FLOOD_TWO_PHASE)
