@@ -457,11 +457,13 @@ def run_ours(args, rank, world, local):
     replay_tb = graph_of(torch, tb_launches)
     bits_ms = _time(torch, stream, replay_tb, reps=4, warmup=2) / TB_LAUNCHES  # per launch
     # its bound is the integer/logic pipe, not HBM: per word (32 cells) and generation the source
-    # issues 13 logic instructions (11 lop3 + 2 funnel shifts: the row summaries and the
-    # bit-sliced count and rule); the pipe retires 64 such lanes per SM and clock
+    # issues 11 lop3 on that pipe (2 for the row summary, 6 for the bit-sliced count, 3 for the
+    # reference rule); its 2 funnel shifts run on the FMA pipe (ncu pipe counters: replacing them
+    # by integer multiply-adds left the logic pipe's instruction count unchanged).  The logic pipe
+    # retires 64 lanes per SM and clock
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     word_gens = (N // 32) * TB_GENS
-    logic_ops = 13 * word_gens
+    logic_ops = 11 * word_gens
     ops_achieved = logic_ops / (bits_ms * 1e-3) / 1e12  # Tops/s
     bits_bytes = N * 3 / 8 * TB_GENS
     bits_achieved = bits_bytes / (bits_ms * 1e-3) / 1e9
@@ -516,8 +518,9 @@ def run_ours(args, rank, world, local):
         "roofline": {"bound": "alu", "achieved": ops_achieved, "peak": alu_peak, "unit": "Tops/s",
                      "frac": ops_achieved / alu_peak, "traffic": profiled_traffic("life_bits_tb"),
                      "kernel": "life_bits_tb", "generations_per_launch": TB_GENS,
-                     "ops": "32-bit integer logic instructions (lop3, funnel shift), per lane",
-                     "ops_per_word_generation": 13, "algorithmic_ops_per_launch": logic_ops,
+                     "ops": "32-bit lop3 instructions per lane (the logic pipe; the row summary's funnel shifts "
+                            "run on the FMA pipe)",
+                     "ops_per_word_generation": 11, "algorithmic_ops_per_launch": logic_ops,
                      "avg_launch_ms": bits_ms, "launches_per_step": GOL_GENS // TB_GENS,
                      "launch_timing": "CUDA graph of %d back-to-back launches" % TB_LAUNCHES,
                      "peak_source": "%d SMs x 64 logic lanes per clock x %.0f MHz (median SM clock of the timed region)"
