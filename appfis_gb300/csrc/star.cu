@@ -200,8 +200,6 @@ template <> struct Vec4<__half> {
 };
 
 __device__ __forceinline__ float f4(const float4& v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w)); }
-// lanes (c, c+1) of v, c = 0 or 2
-__device__ __forceinline__ float2 pair(const float4& v, int c) { return c == 0 ? make_float2(v.x, v.y) : make_float2(v.z, v.w); }
 
 template <class T, int MODE>
 __global__ void __launch_bounds__(256) star_r4_vec(const T* __restrict__ in, T* __restrict__ out, int nx, int ny, int nz, int px,
