@@ -2,8 +2,8 @@
 fault or hang: every wait involved has a limit, the kernel gives up, the call reports
 APPFIS_GB_ETIMEOUT, and the next call on the same device computes the right answer.
 
-* The persistent flood kernel's grid barrier: CTA 0 does not arrive at the first barrier and
-  each barrier wait gives up after 4096 polls (~64 ns sleep each).
+* The persistent flood kernels' grid barrier (fused and two-phase forms): CTA 0 does not arrive
+  at the first barrier and each barrier wait gives up after 4096 polls (~64 ns sleep each).
 * The TMA-staged radius-4 star: each CTA arms its first plane's mbarrier for 16 bytes more than
   the copy delivers and waits at most 1 ms; it then lets its copies land (10 ms per pending
   plane) and leaves; appfis_gb_stream_sync reads the device status word."""
@@ -19,16 +19,17 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 
-def test_flood_grid_barrier_wait_runs_out_then_recovers(gb, torch_cuda):
+@pytest.mark.parametrize("flags", [_lib.FLOOD_FUSED, _lib.FLOOD_TWO_PHASE])
+def test_flood_grid_barrier_wait_runs_out_then_recovers(gb, torch_cuda, flags):
     doms = [W.triton_domain(70, 50, 3), W.triton_domain(40, 64, 4)]
     args = (10.0, 0.5, 1e-3, 0.035, 600.0, 600.0, 1.0)
     gb.call("appfis_gb_test_stall_next", 1, 4096)
     with pytest.raises(_lib.AppfisError) as e:
-        _lib.flood_job(doms, *args, max_steps=30, dtype=_lib.F32)
+        _lib.flood_job(doms, *args, max_steps=30, dtype=_lib.F32, flags=flags)
     assert e.value.status == _lib.ETIMEOUT, str(e.value)
     # the plan is used up: the same run now completes and matches a clean run's fields
-    a = _lib.flood_job(doms, *args, max_steps=30, dtype=_lib.F32)
-    b = _lib.flood_job(doms, *args, max_steps=30, dtype=_lib.F32)
+    a = _lib.flood_job(doms, *args, max_steps=30, dtype=_lib.F32, flags=flags)
+    b = _lib.flood_job(doms, *args, max_steps=30, dtype=_lib.F32, flags=flags)
     assert a["steps"] == b["steps"] == [30, 30]
     for k in range(2):
         assert np.array_equal(a["h"][k], b["h"][k])
