@@ -22,6 +22,7 @@
 // which bounds the FP16 error to the last period's correction.  The sweep's own ss is
 // (e' - e)/w (FP32, before rounding e').  Inner sweeps: himeno_mixed2 (TMA-staged, two points
 // per thread) when the FP16 rows are 16-byte aligned, else himeno_ring<1>.
+#include <cstdlib>
 #include <cuda_fp16.h>
 
 #include <type_traits>
@@ -1044,11 +1045,18 @@ int appfis_gb_himeno(const float* const* coef, float* p, float* wrk2, int nx, in
                                  ny + 2, TmaLayout::W, RY + 2));
         unsigned* status;
         GB_TRY(gb::status_word(&status));
-        const int kz = gb::balanced_chunk(nz, HKZ);
-        dim3 tgrd(nx / RX + 1, gb::ceil_div(ny, RY), gb::ceil_div(nz, kz));
-        GB_TRY(gs.init(dev_gosa, (size_t)tgrd.x * tgrd.y * tgrd.z, 1));
         constexpr int smem = TmaLayout::smem(TMA_S_PLAIN);
         GB_CUDA(cudaFuncSetAttribute(himeno_tma<TMA_S_PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        // z chunks of 16-48 planes whose grid fills the resident CTAs in whole waves (each chunk
+        // re-reads 2 halo planes of p)
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, himeno_tma<TMA_S_PLAIN>, RX * RY, smem) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        const long long cols = (long long)(nx / RX + 1) * gb::ceil_div(ny, RY);
+        const int kz = gb::wave_chunk(nz, 16, 48, cols, (long long)per_sm * gb::sm_count(), 2);
+        dim3 tgrd(nx / RX + 1, gb::ceil_div(ny, RY), gb::ceil_div(nz, kz));
+        GB_TRY(gs.init(dev_gosa, (size_t)tgrd.x * tgrd.y * tgrd.z, 1));
         for (int it = 0; it < iters; it++) {
             himeno_tma<TMA_S_PLAIN><<<tgrd, blk, smem, st>>>(maps[ci], buf[1 - ci], nx, ny, nz, pitch, ny + 2, kz, omega,
                                                             gs.next(tgrd, 1, dev_gosa ? dev_gosa + it : nullptr), status);
