@@ -22,7 +22,6 @@
 // which bounds the FP16 error to the last period's correction.  The sweep's own ss is
 // (e' - e)/w (FP32, before rounding e').  Inner sweeps: himeno_mixed2 (TMA-staged, two points
 // per thread) when the FP16 rows are 16-byte aligned, else himeno_ring<1>.
-#include <cstdlib>
 #include <cuda_fp16.h>
 
 #include <type_traits>
