@@ -1182,7 +1182,17 @@ int appfis_gb_himeno_mixed_ex(const float* const* coef, float* p, float* p_work,
     float* P[2] = {p, p_work};
     // correction maps: [P buffer][e buffer]
     CorrMaps cmaps[2][2];
-    dim3 cgrd(nx / RX + 1, gb::ceil_div(ny, RY), gb::ceil_div(nz, tkz));
+    constexpr int csmem = corr_smem(CORR_S);
+    int ckz = tkz;  // the correction pass's own z chunk: whole waves of its resident CTAs
+    if (use_tma) {
+        GB_CUDA(cudaFuncSetAttribute(himeno_correct_tma<CORR_S>, cudaFuncAttributeMaxDynamicSharedMemorySize, csmem));
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, himeno_correct_tma<CORR_S>, RX * RY, csmem) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        ckz = gb::wave_chunk(nz, 16, 64, (long long)(nx / RX + 1) * gb::ceil_div(ny, RY), (long long)per_sm * gb::sm_count(), 2);
+    }
+    dim3 cgrd(nx / RX + 1, gb::ceil_div(ny, RY), gb::ceil_div(nz, ckz));
     GosaSeq gs;  // block sums of the sweeps and of the correction passes (which do a sweep each)
     {
         const unsigned nb1 = use_tma ? tgrd.x * tgrd.y * tgrd.z : rgrd.x * rgrd.y * rgrd.z;
@@ -1190,7 +1200,6 @@ int appfis_gb_himeno_mixed_ex(const float* const* coef, float* p, float* p_work,
         const unsigned nb3 = use_tma ? cgrd.x * cgrd.y * cgrd.z : grd.x * grd.y * grd.z;
         GB_TRY(gs.init(dev_gosa, std::max(std::max(nb1, nb2), nb3), 1));
     }
-    constexpr int csmem = corr_smem(CORR_S);
     if (use_tma) {
         const int py = ny + 2;
         for (int n = 0; n < 12; n++)
@@ -1203,7 +1212,6 @@ int appfis_gb_himeno_mixed_ex(const float* const* coef, float* p, float* p_work,
                 GB_TRY(gb::tensor_map_3d(&cmaps[a][b].m[13], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, E[b], nx + 2, py, nz + 2, pitch, py, 48,
                                          RY + 2));
             }
-        GB_CUDA(cudaFuncSetAttribute(himeno_correct_tma<CORR_S>, cudaFuncAttributeMaxDynamicSharedMemorySize, csmem));
     }
     int pc = 0, ec = 0;
     const float inv_omega = 1.0f / omega;
@@ -1214,7 +1222,7 @@ int appfis_gb_himeno_mixed_ex(const float* const* coef, float* p, float* p_work,
         const GosaIO gz = gs.next(use_tma ? cgrd : grd, 1, prime ? g : nullptr);
         if (use_tma)
             himeno_correct_tma<CORR_S><<<cgrd, rblk, csmem, st>>>(cmaps[pc][ec], P[1 - pc], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2,
-                                                                 tkz, omega, inv_omega, prime ? 1 : 0, gz, status);
+                                                                 ckz, omega, inv_omega, prime ? 1 : 0, gz, status);
         else
             himeno_correct<HBX, HBY><<<grd, blk, 0, st>>>(cf, P[pc], E[ec], P[1 - pc], Dd, E[1 - ec], nx, ny, nz, pitch, ny + 2,
                                                           HKZ, omega, inv_omega, prime ? 1 : 0, gz);
