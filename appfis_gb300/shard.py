@@ -1,5 +1,6 @@
 """Multi-rank decomposition of the hot path: slabs of a padded field with a halo exchange per
-sweep, scalar all-reduces, and the assignment of independent flood domains to ranks.
+sweep (or one exchange of a deeper halo per several sweeps), scalar all-reduces, and the
+assignment of independent flood domains to ranks.
 
 The reference partitions every grid into Cartesian blocks, one per MPI rank
 (Appfis/Common.hpp:197-226: n // blocks points per rank, the first n % blocks ranks one more),
@@ -129,6 +130,34 @@ def iterate(slab, cur, nxt, iters, sweep):
         slab.exchange(cur)
         sweep(cur, nxt)
         cur, nxt = nxt, cur
+    return cur
+
+
+def iterate_blocked(slab, cur, nxt, iters, sweep_layers, depth):
+    """`iters` sweeps of a radius-1 stencil with one ghost exchange per `depth` sweeps (temporal
+    blocking across ranks; slab.ghost >= depth): after an exchange the rank advances its whole
+    local slab except the outermost layer on each side that faces a neighbour by up to `depth`
+    sweeps.  The stale outer layer corrupts one more layer per sweep, so after k <= ghost
+    sweeps the rank's own layers are exact, and the next exchange replaces the corrupted ghost
+    layers.  On a side without a neighbour (non-periodic edge) all ghost layers stay fixed, as
+    the reference's boundary does.  This lets a kernel that does several sweeps per launch on
+    chip (the time-blocked heat and GameOfLife kernels) run on a slab.
+
+    sweep_layers(cur, nxt, k, lo, hi) advances layers lo .. hi-1 of `cur` (slowest axis) by k
+    sweeps, reading the layers outside that range as a fixed boundary, and returns the buffer
+    holding the result (cur or nxt; its layers outside lo .. hi-1 must equal cur's).  Returns
+    the buffer holding the newest state."""
+    if not 1 <= depth <= slab.ghost:
+        raise ValueError("iterate_blocked: depth %d must be in 1 .. ghost width %d" % (depth, slab.ghost))
+    lo = 1 if slab.low is not None else slab.ghost
+    hi = slab.local_extent() - (1 if slab.high is not None else slab.ghost)
+    done = 0
+    while done < iters:
+        k = min(depth, iters - done)
+        slab.exchange(cur)
+        if sweep_layers(cur, nxt, k, lo, hi) is nxt:
+            cur, nxt = nxt, cur
+        done += k
     return cur
 
 

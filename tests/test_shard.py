@@ -1,6 +1,7 @@
 """Multi-rank path on host ranks (gloo, 2 and 3 processes): the reference's block partition,
-the two-phase ghost exchange (periodic and not), a sharded heat run gathered and compared
-bit-for-bit with the whole-grid oracle, scalar all-reduce, and the flood domain plan.
+the two-phase ghost exchange (periodic and not), sharded heat runs (one exchange per sweep, and
+one exchange of a 3-deep halo per 1-3 sweeps) gathered and compared bit-for-bit with the
+whole-grid oracle, scalar all-reduce, and the flood domain plan.
 
 The per-rank sweep in these tests is the oracle's one-iteration step (no GPU here); on GPUs the
 same driver calls the C-ABI sweep (tests/test_shard_gpu.py)."""
@@ -103,6 +104,45 @@ def _case_heat(rank, world):
         return None
     ref = O.heat2d(full.numpy(), c["iters"], c["r"], threads=1)
     return bool(np.array_equal(got.numpy(), ref[1:-1])), total, float(ref[1:-1, 1:-1].astype(np.float64).sum())
+
+
+def _case_heat_blocked(rank, world):
+    """Ghost width 3, one exchange per `depth` sweeps, 10 sweeps (the last block shorter)."""
+    from oracle import oracle as O
+    c = dict(nx=37, ny=29, iters=10, r=0.2)
+    out = []
+    for depth in (1, 2, 3):
+        g = 3
+        core = W.heat2d_padded(c["nx"], c["ny"], 1.0, 7)
+        # the global field with g ghost rows on each side (the Dirichlet row next to the interior)
+        full = torch.from_numpy(np.concatenate([np.repeat(core[:1], g - 1, 0), core, np.repeat(core[-1:], g - 1, 0)]))
+        s = shard.Slab(c["ny"], g)
+        a = s.scatter(full)
+        b = a.clone()
+
+        def sweep_layers(cur, nxt, k, lo, hi):  # rows lo .. hi-1, rows lo-1 and hi as the fixed ring
+            sub = cur[lo - 1:hi + 1].numpy()
+            nxt.copy_(cur)
+            nxt[lo - 1:hi + 1] = torch.from_numpy(O.heat2d(sub, k, c["r"], threads=1))
+            return nxt
+
+        cur = shard.iterate_blocked(s, a, b, c["iters"], sweep_layers, depth)
+        got = s.gather(cur)
+        if rank == 0:
+            ref = O.heat2d(core, c["iters"], c["r"], threads=1)
+            out.append(bool(np.array_equal(got.numpy(), ref[1:-1])))
+    return out if rank == 0 else None
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_blocked_exchange_heat_matches_whole_grid_gloo(world):
+    assert _spawn(_case_heat_blocked, world) == [True, True, True]
+
+
+def test_blocked_depth_checked():
+    s = shard.Slab(10, 2, rank=0, world=1)
+    with pytest.raises(ValueError):
+        shard.iterate_blocked(s, torch.zeros(14), torch.zeros(14), 3, lambda *a: None, 3)
 
 
 @pytest.mark.parametrize("world", [2, 3])
