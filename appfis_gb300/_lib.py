@@ -82,6 +82,7 @@ class FloodParams(ctypes.Structure):
 FLOOD_SKIP_DRY = 1
 FLOOD_TWO_PHASE = 2
 FLOOD_FUSED = 4
+FLOOD_UNSTAGED = 8
 
 
 def flood_job(domains, dx, courant, hextra, manning, t_end, print_interval=None, time_step=1.0, max_steps=0,

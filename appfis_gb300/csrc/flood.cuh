@@ -14,6 +14,7 @@
 #pragma once
 
 #include "flood_core.cuh"
+#include "tma.cuh"
 
 namespace flood {
 
@@ -59,6 +60,9 @@ struct Params {
     unsigned long long spin_limit;  // polls before a grid-barrier wait gives up
     int stall_cta;                  // testing: this CTA skips its arrival at the first barrier (-1: none)
     const SrcDev* srcs;             // [ndom] point sources, or null (no source phase)
+    const CUtensorMap* maps;        // staged fused pass: [ndom][8] row maps (h0 h1 qx0 qx1 qy0 qy1 dem n2)
+    unsigned long long wait_ns;     // staged: limit of one wait for a stage of rows
+    unsigned tx_extra;              // testing: bytes added to each warp's first stage (it cannot complete)
 };
 
 constexpr unsigned long long SPIN_LIMIT = 1ull << 25;
@@ -517,11 +521,35 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
 // two-phase kernel's: the same face, update, fix and dt functions of the same values.
 constexpr int FCOLS = 28;
 
+// Staged rows (FP32, rows 16-byte aligned): each warp streams its strip's rows of the five
+// input arrays (h, qx, qy of the step's state, dem, n2) into its own ring of FS_NS shared-memory
+// stages by TMA, FS_TR rows per stage and array as a 36-column box whose origin, the strip's
+// first column rounded down to a multiple of 4, is 16-byte aligned.  A stage's slot is refilled
+// with the stage FS_NS further on as soon as its last row is read, so FS_NS - 1 stages are in
+// flight while the warp computes, and no row is held in registers ahead of its use.  Cells
+// outside the padded domain arrive as the boxes' zero fill.
+constexpr int FS_TR = 4, FS_NS = 2, FS_BW = 36;
+constexpr int FS_ABYTES = (FS_BW * FS_TR * 4 + 127) / 128 * 128;  // one array's box, 128-byte aligned
+constexpr int FS_STAGE = 5 * FS_ABYTES;
+constexpr int FS_WARPS = 8;  // warps per CTA (256 threads)
+constexpr int FS_SMEM = FS_WARPS * FS_NS * FS_STAGE + FS_WARPS * FS_NS * 8;
+constexpr unsigned FS_TX = 5u * FS_BW * FS_TR * 4u;  // bytes one stage's five boxes deliver
+
+struct RowRing {
+    unsigned char* buf;  // this warp's FS_NS stages
+    uint64_t* bar;       // their barriers
+    unsigned g;          // stages consumed by this warp so far: slot g % FS_NS, phase (g / FS_NS) & 1
+    bool dead;           // a wait gave up: the warp does no further work (the run reports the error)
+};
+
 // D is the CTA's shared-memory copy of the domain descriptor, taken by reference: its eight
 // array pointers are then read from shared memory where they are used instead of occupying 16
 // registers for the whole strip (90.5 against 87.4 G cell-steps/s on the 32-domain batch).
-template <class T>
-__device__ bool phase_bf(const Dom<T>& D, long long local, int b, T dt, const Params& p, unsigned long long* dt_next)
+// STAGED: rows come from the warp's TMA ring (`ring`, domain d's maps in p.maps); otherwise
+// from global memory, the row after next loaded while a row is computed.
+template <class T, bool STAGED = false>
+__device__ bool phase_bf(const Dom<T>& D, long long local, int b, T dt, const Params& p, unsigned long long* dt_next,
+                         RowRing* ring = nullptr, int d = 0, Ctl* ctl = nullptr)
 {
     const int lane = threadIdx.x & 31;
     const int loc = (int)local, sy = loc / D.strips_x, sx = loc - sy * D.strips_x;  // 32-bit: a domain has < 2^31 strips
@@ -549,12 +577,56 @@ __device__ bool phase_bf(const Dom<T>& D, long long local, int b, T dt, const Pa
         return Raw<T>{h[c], qx[c], qy[c], dem[c]};
     };
     const int ra = j0 - 1, rb = j1;  // rows updated (those outside 1..ny keep their state)
-    Cell<T> cj = cell_of(raw(ra));
-    Raw<T> rn = raw(ra + 1);
+    // staged rows: strip rows ra-1 .. rb+1 (x = 0 .. nrow-1) in stages of FS_TR, read in order
+    const int x0 = max(sx * FCOLS - 4, 0), off = i - x0;  // box origin column; this lane's column in the box
+    const int y0 = ra - 1, nrow = rb - ra + 3, nst = (nrow + FS_TR - 1) / FS_TR;
+    bool bad = false;  // staged: a wait gave up (warp-uniform)
+    int issued = -1;   // staged: last stage issued
+    auto issue = [&](int q) {  // warp-collective: stage q of the strip into its slot
+        const unsigned G = ring->g + q, s = G % FS_NS;
+        if (lane == 0) gb::tma::arrive_expect(&ring->bar[s], FS_TX + (G == 0 ? p.tx_extra : 0u));
+        __syncwarp();
+        if (lane < 5) {  // one array per lane: h, qx, qy of buffer b, dem, n2
+            const CUtensorMap* mp = p.maps + (size_t)d * 8 + (lane < 3 ? 2 * lane + b : lane + 3);
+            gb::tma::load_3d(ring->buf + s * FS_STAGE + lane * FS_ABYTES, mp, x0, y0 + q * FS_TR, 0, &ring->bar[s]);
+        }
+        issued = q;
+    };
+    // staged row x of the strip (state, and n2 into n2o); called once per row, in row order
+    auto fetch = [&](int x, T& n2o) -> Raw<T> {
+        const int q = x / FS_TR, rr = x - q * FS_TR;
+        const unsigned G = ring->g + q, s = G % FS_NS;
+        if (rr == 0 && !bad) bad = __any_sync(0xffffffffu, !gb::tma::wait(&ring->bar[s], (G / FS_NS) & 1u, p.wait_ns));
+        const T* a = reinterpret_cast<const T*>(ring->buf + s * FS_STAGE) + rr * FS_BW + off;
+        const int r = y0 + x;
+        Raw<T> v = zr;
+        if (col && r >= 0 && r <= ny + 1) v = Raw<T>{a[0], a[FS_ABYTES / 4], a[2 * FS_ABYTES / 4], a[3 * FS_ABYTES / 4]};
+        n2o = upd && r >= 1 && r <= ny ? a[4 * FS_ABYTES / 4] : zero;
+        if (rr == FS_TR - 1) {  // the stage is read: its slot takes stage q + FS_NS
+            __syncwarp();
+            if (!bad && q + FS_NS < nst) issue(q + FS_NS);
+        }
+        return v;
+    };
+    Cell<T> cj;
+    Raw<T> rn;
+    T n2c = zero;  // staged: n2 of row r
+    Cell<T> cm;
+    if constexpr (STAGED) {
+        if (ring->dead) return false;
+        __syncwarp();  // every lane is done with the previous strip's stages before their slots refill
+        for (int q = 0; q < FS_NS && q < nst; q++) issue(q);
+        T unused;
+        cm = cell_of(fetch(0, unused));
+        cj = cell_of(fetch(1, n2c));
+    } else {
+        cj = cell_of(raw(ra));
+        rn = raw(ra + 1);
+    }
     T ycar[3] = {zero, zero, zero};  // rhs0 Y part of row r (from face r|r-1)
     bool ywet = false;
     if (upd && ra >= 1) {
-        const Cell<T> cm = cell_of(raw(ra - 1));
+        if constexpr (!STAGED) cm = cell_of(raw(ra - 1));
         T r2[3];
         ywet = face<T>(cj, cm, zero, one, dx, dt, hextra, ycar, r2);
     }
@@ -563,9 +635,16 @@ __device__ bool phase_bf(const Dom<T>& D, long long local, int b, T dt, const Pa
     T mn = K<T>::big();
     bool dry = true;  // every cell this lane owns ends with h = qx = qy = 0
     for (int r = ra; r <= rb; r++) {
-        const Raw<T> rnn = r + 2 <= rb + 1 ? raw(r + 2) : zr;  // prefetch
         const bool rin = r >= 1 && r <= ny;
-        const T n2v = upd && rin ? n2[(size_t)r * px + i] : zero;
+        Raw<T> rnn;
+        T n2v, n2n = zero;
+        if constexpr (STAGED) {
+            rn = fetch(r + 1 - y0, n2n);
+            n2v = n2c;
+        } else {
+            rnn = r + 2 <= rb + 1 ? raw(r + 2) : zr;  // prefetch
+            n2v = upd && rin ? n2[(size_t)r * px + i] : zero;
+        }
         const Cell<T> cn_ = cell_of(rn);
         // X face i|i+1 of row r: rhs0 of cell i, rhs1 of cell i+1 (the next lane)
         const Cell<T> right = shfl_cell(cj, 1, true);
@@ -626,7 +705,26 @@ __device__ bool phase_bf(const Dom<T>& D, long long local, int b, T dt, const Pa
         qy1 = qyn;
         z1 = cj.z;
         cj = cn_;
-        rn = rnn;
+        if constexpr (STAGED) {
+            n2c = n2n;
+        } else {
+            rn = rnn;
+        }
+    }
+    if constexpr (STAGED) {
+        if (bad) {  // report, and let the copies still in flight land before the warp moves on
+            if (lane == 0) {
+                atomicExch(&ctl->error, 1);
+                for (int q = max(0, issued - FS_NS + 1); q <= issued; q++) {
+                    const unsigned G = ring->g + q;
+                    gb::tma::wait(&ring->bar[G % FS_NS], (G / FS_NS) & 1u, gb::tma::DRAIN_NS);
+                }
+            }
+            __syncwarp();
+            ring->dead = true;
+            return false;
+        }
+        ring->g += nst;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -641,12 +739,28 @@ __device__ bool phase_bf(const Dom<T>& D, long long local, int b, T dt, const Pa
 // state, then one pass and one grid barrier per step.  The per-domain CFL minimum of step n is
 // accumulated in dtbits[n % 3] during step n-1, read at the start of step n, and the slot of
 // step n+2 is reset by block 0 during step n (nobody reads or writes it then).
-template <class T, bool SKIP>
+// STAGED: the step's rows arrive through each warp's TMA ring (FS_SMEM bytes of dynamic shared
+// memory; FP32 domains whose rows are 16-byte aligned).
+template <class T, bool SKIP, bool STAGED = false>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1) flood_fused(const Dom<T>* __restrict__ gdoms, Ctl* ctl,
                                                                                           Params p)
 {
     __shared__ Dom<T> doms[MAXD];
     __shared__ DomCtl<T> dc;
+    extern __shared__ __align__(128) unsigned char fsm[];
+    RowRing ring = {nullptr, nullptr, 0u, false};
+    if constexpr (STAGED) {
+        const int w = threadIdx.x >> 5;
+        ring.buf = fsm + w * (FS_NS * FS_STAGE);
+        ring.bar = reinterpret_cast<uint64_t*>(fsm + FS_WARPS * FS_NS * FS_STAGE) + w * FS_NS;
+        if (gb::tma::smem_u32(fsm) & 127u) {  // the boxes need 128-byte aligned slots: do no work
+            ring.dead = true;
+            if (threadIdx.x == 0) atomicExch(&ctl->error, 3);
+        } else if ((threadIdx.x & 31) == 0) {
+            for (int k = 0; k < FS_NS; k++) gb::tma::bar_init(&ring.bar[k], 1);
+            gb::tma::fence_init();
+        }
+    }
     for (int k = threadIdx.x; k < p.ndom; k += blockDim.x) doms[k] = gdoms[k];
     __syncthreads();
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -694,10 +808,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
                     if (lane == 0) zout[s] = z;
                     return;
                 }
-                const bool dry = phase_bf<T>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p, &ctl->dtbits[dn][d]);
+                const bool dry = phase_bf<T, STAGED>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p, &ctl->dtbits[dn][d],
+                                                     &ring, d, ctl);
                 if (lane == 0) zout[s] = dry ? (unsigned char)(z < 2 ? z + 1 : 2) : 0;
             } else if (f & 4) {
-                phase_bf<T>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p, &ctl->dtbits[dn][d]);
+                phase_bf<T, STAGED>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p, &ctl->dtbits[dn][d], &ring, d, ctl);
             }
         });
         if (blockIdx.x == 0 && threadIdx.x == 0) {  // commit the per-domain scalars of step n

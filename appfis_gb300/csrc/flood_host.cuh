@@ -57,7 +57,10 @@ static __global__ void flood_results(const Ctl* __restrict__ ctl, int ndom, int*
         if (simtime) simtime[d] = ctl->simtime[0][d];
     }
     if (d == 0 && status)
-        *status = ctl->error == 0 ? APPFIS_GB_OK : (ctl->error == 2 ? APPFIS_GB_ENUMERIC : APPFIS_GB_ETIMEOUT);
+        *status = ctl->error == 0   ? APPFIS_GB_OK
+                  : ctl->error == 2 ? APPFIS_GB_ENUMERIC
+                  : ctl->error == 3 ? APPFIS_GB_ECUDA  // staging buffers misaligned: no step was taken
+                                    : APPFIS_GB_ETIMEOUT;
 }
 
 // scols: interior columns per strip (SCOLS for the two-phase kernel, FCOLS for the fused one).
@@ -211,7 +214,42 @@ int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_para
     p.zc = nullptr;
     p.spin_limit = SPIN_LIMIT;
     p.stall_cta = -1;
+    p.maps = nullptr;
+    p.wait_ns = 1000000000ull;
+    p.tx_extra = 0;
     GB_TRY(upload_sources(doms, srcs, ndom, &p.srcs, st));
+    // the fused FP32 full sweep stages its rows by TMA when every domain's arrays and rows are
+    // 16-byte aligned: 107.6 against 92.6 G cell-steps/s on the 32-domain batch.  With dry strips
+    // left out it loads them directly (324 against 319: a warp's strips are then scattered, and
+    // each one starts its ring from empty); so does UNSTAGED, or any other layout (same fields).
+    bool staged = fused && std::is_same<T, float>::value && !(prm->flags & APPFIS_GB_FLOOD_UNSTAGED) &&
+                  !(prm->flags & APPFIS_GB_FLOOD_SKIP_DRY);
+    for (int d = 0; staged && d < ndom; d++) {
+        const Dom<T>& D = tab[d];
+        const void* a[8] = {D.h[0], D.h[1], D.qx[0], D.qx[1], D.qy[0], D.qy[1], D.dem, D.n2};
+        for (int k = 0; k < 8; k++) staged = staged && gb::aligned16(a[k]);
+        staged = staged && (D.px * sizeof(T)) % 16 == 0;
+    }
+    if (staged) {
+        std::vector<CUtensorMap> maps(8 * (size_t)ndom);
+        for (int d = 0; d < ndom; d++) {
+            const Dom<T>& D = tab[d];
+            const void* a[8] = {D.h[0], D.h[1], D.qx[0], D.qx[1], D.qy[0], D.qy[1], D.dem, D.n2};
+            for (int k = 0; k < 8; k++)
+                GB_TRY(gb::tensor_map_3d(&maps[8 * d + k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, sizeof(T), a[k], D.nx + 2, D.ny + 2, 1,
+                                         D.px, D.ny + 2, FS_BW, FS_TR));
+        }
+        void* dm;
+        GB_TRY(gb::workspace(gb::WS_FLOOD_MAPS, sizeof(CUtensorMap) * maps.size(), &dm));
+        GB_CUDA(cudaMemcpyAsync(dm, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice, st));
+        GB_CUDA(cudaStreamSynchronize(st));  // the host copy is a local
+        p.maps = reinterpret_cast<const CUtensorMap*>(dm);
+        unsigned long long test_ns = 0;
+        if (gb::take_test_stall(gb::TEST_TMA_SHORTFALL, &test_ns)) {  // a test runs the first stage's waits out
+            p.wait_ns = test_ns;
+            p.tx_extra = 16;
+        }
+    }
     unsigned long long test_limit = 0;
     if (gb::take_test_stall(gb::TEST_FLOOD_BARRIER, &test_limit)) {  // a test runs a barrier wait out
         p.spin_limit = test_limit;
@@ -226,9 +264,12 @@ int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_para
 
     int dev = 0, per_sm = 0;
     GB_CUDA(cudaGetDevice(&dev));
-    auto kern = fused ? (p.zc ? flood_fused<T, true> : flood_fused<T, false>)
-                      : (p.zc ? flood_persistent<T, true> : flood_persistent<T, false>);
-    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
+    auto kern = staged  ? flood_fused<T, false, true>
+                : fused ? (p.zc ? flood_fused<T, true> : flood_fused<T, false>)
+                        : (p.zc ? flood_persistent<T, true> : flood_persistent<T, false>);
+    const int smem = staged ? FS_SMEM : 0;
+    if (staged) GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem));
     if (per_sm < 1) return gb::fail(APPFIS_GB_ECUDA, "flood: kernel cannot be resident");
     long long want = (total * 32 + 255) / 256;  // one warp per strip at most
     int grid = (int)std::min<long long>(want, (long long)per_sm * gb::sm_count());
@@ -236,7 +277,7 @@ int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_para
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(256);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
@@ -340,7 +381,8 @@ int job(int ndom, const int* nx, const int* ny, const double* const* dem, double
     GB_CUDA(cudaStreamSynchronize(st));
     if (steps[ndom] != APPFIS_GB_OK)
         return gb::fail(steps[ndom], steps[ndom] == APPFIS_GB_ENUMERIC ? "flood: the time step collapsed (zero or NaN)"
-                                                                       : "flood: a grid-wide wait timed out");
+                                     : steps[ndom] == APPFIS_GB_ECUDA  ? "flood: row staging buffers misaligned"
+                                                                       : "flood: a device-side wait timed out");
     if (mass_out) {
         GB_TRY(mass<T>(doms.data(), ndom, steps.data(), dmass, st));
         std::vector<double> m1(ndom);

@@ -25,7 +25,7 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 
 // Device workspace: one grow-only allocation per (device, slot), reused across calls.  Calls
 // that use the same slot on the same device must not overlap on the GPU.
-enum Slot { WS_REDUCE = 0, WS_JOB_A, WS_JOB_B, WS_JOB_C, WS_JOB_D, WS_JOB_E, WS_JOB_F, WS_LIFE_C, WS_LIFE_D, WS_LIFE_E, WS_LIFE_F, WS_FLOOD_Z, WS_FLOOD_SRC, WS_F64_PARTIALS, WS_SLOTS };
+enum Slot { WS_REDUCE = 0, WS_JOB_A, WS_JOB_B, WS_JOB_C, WS_JOB_D, WS_JOB_E, WS_JOB_F, WS_LIFE_C, WS_LIFE_D, WS_LIFE_E, WS_LIFE_F, WS_FLOOD_Z, WS_FLOOD_SRC, WS_F64_PARTIALS, WS_FLOOD_MAPS, WS_SLOTS };
 int workspace(int slot, size_t bytes, void** out);
 // Pinned host staging buffer, grow-only, per slot (0..1).
 int pinned(int slot, size_t bytes, void** out);

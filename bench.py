@@ -854,6 +854,11 @@ def bench_flood(torch, gb, W, dev, sp):
         return torch.stack([bufs[k][b], bufs[k][2 + b], bufs[k][4 + b]])[:, 1:ny + 1, 1:nx + 1]
 
     dense = [final_state(k, st[k]).clone() for k in range(nd)]
+    # the same fused pass loading its rows directly instead of staging them by TMA
+    prm.flags = _lib.FLOOD_UNSTAGED
+    ms_u = _time(torch, sp, batched, reps=1)
+    same_u = bool((steps.cpu().numpy().astype(np.int64) == st).all()) and all(
+        torch.equal(final_state(k, st[k]), dense[k]) for k in range(nd))
     # the two-pass form of the same full sweep (fix + dt, then update; bit-identical fields)
     prm.flags = _lib.FLOOD_TWO_PHASE
     ms_2 = _time(torch, sp, batched, reps=1)
@@ -909,10 +914,14 @@ def bench_flood(torch, gb, W, dev, sp):
     g_2 = cell_steps * 48 / ((ms_2 - setup_ms) * 1e-3) / 1e9  # two passes: 16 B + 32 B
     return {"workload": "flood model, 32 domains (sides 512-3072, %.1f M cells), fractal DEM, to t = 600 s" % (cells.sum() / 1e6),
             "batched_fp32": {"glups": cell_steps / ((ms_b - setup_ms) * 1e-3) / 1e9, "ms": ms_b - setup_ms,
-                             "kernel": "flood_fused (one pass per step)", "bytes_per_cell_step": 32, "achieved_gbs": g_b,
+                             "kernel": "flood_fused (one pass per step; rows staged by TMA, 4-row stages)",
+                             "bytes_per_cell_step": 32, "achieved_gbs": g_b,
                              "frac_of_hbm": g_b / hbm,
                              "steps_min": int(st.min()), "steps_max": int(st.max()), "cell_steps": cell_steps,
                              "mass_rel_change_max": drift, "error_vs_fp64": err_flood},
+            "batched_fp32_row_loads": {"glups": cell_steps / ((ms_u - setup_ms) * 1e-3) / 1e9, "ms": ms_u - setup_ms,
+                                       "kernel": "flood_fused, rows loaded directly (APPFIS_GB_FLOOD_UNSTAGED)",
+                                       "fields_identical_to_staged": same_u},
             "batched_fp32_two_phase": {"glups": cell_steps / ((ms_2 - setup_ms) * 1e-3) / 1e9, "ms": ms_2 - setup_ms,
                                        "kernel": "flood_persistent (fix + dt, then update)", "bytes_per_cell_step": 48,
                                        "achieved_gbs": g_2, "frac_of_hbm": g_2 / hbm, "fields_identical_to_fused": same2},
@@ -989,7 +998,8 @@ def profile_case(name, local):
     himeno-small: 129x129x257, the mixed form with one inner sweep per launch (himeno_mixed2),
             then with two (himeno_mixed_tb2), 4 sweeps each (~0.3 GB)
     flood:  the 32-domain batch (80 M cells, ~2.6 GB), 20 steps (one flood_fused launch)
-    flood-small: the first 6 domains of the batch (15.8 M cells), 20 steps (one flood_fused launch)"""
+    flood-small: the first 6 domains of the batch (15.8 M cells), 20 steps (one flood_fused launch,
+    rows staged by TMA); flood-small-rows: the same with the rows loaded directly"""
     import torch
 
     import appfis_gb300 as gb
@@ -999,14 +1009,14 @@ def profile_case(name, local):
     sp = torch.cuda.current_stream(dev)
     if name != "life":
         fn = {"himeno": bench_himeno, "fdtd": bench_fdtd, "heat": bench_heat}.get(name)
-        if name in ("flood", "flood-small"):
+        if name in ("flood", "flood-small", "flood-small-rows"):
             from appfis_gb300 import _lib
             c = W.TRITON
             doms = W.triton_batch(c["n_domains"], c["side_lo"], c["side_hi"], c["seed"])
-            if name == "flood-small":
+            if name != "flood":
                 doms = doms[:6]
             _lib.flood_job(doms, c["dx"], c["courant"], c["hextra"], c["manning"], c["t_end"], c["t_end"], c["time_step"],
-                           max_steps=20, dtype=_lib.F32)
+                           max_steps=20, dtype=_lib.F32, flags=_lib.FLOOD_UNSTAGED if name == "flood-small-rows" else 0)
         else:
             profile_small(name, torch, gb, W, dev, sp)
         torch.cuda.synchronize(dev)
@@ -1038,7 +1048,8 @@ def main():
     ap.add_argument("--apps", default="heat2d,himeno,fdtd3d,flood", help="comma-separated per-workload measurements")
     ap.add_argument("--apps-unchanged", action="store_true",
                     help="time the reference's sample applications on its CPU path, its GPU path and the drop-in")
-    ap.add_argument("--profile-case", choices=["life", "himeno", "himeno-small", "fdtd", "heat", "flood", "flood-small"], default=None,
+    ap.add_argument("--profile-case", choices=["life", "himeno", "himeno-small", "fdtd", "heat", "flood", "flood-small",
+                                                  "flood-small-rows"], default=None,
                     help="launch a short fixed sequence of the named workload's kernels (for ncu), no timing")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

@@ -75,7 +75,10 @@ APPFIS_GB_API int appfis_gb_stream_sync(void* stream);
  *  kind 2: the next TMA-staged radius-4 star launch (appfis_gb_star_r4): every CTA arms its
  *          first plane's mbarrier for 16 bytes more than the copy delivers, and waits at most
  *          `limit` ns (1e3 .. 1e8) per wait: the launch gives up, lets its copies land, and the
- *          next appfis_gb_stream_sync returns APPFIS_GB_ETIMEOUT.
+ *          next appfis_gb_stream_sync returns APPFIS_GB_ETIMEOUT.  The same plan applies to the
+ *          next flood run that stages its rows by TMA (FP32 fused full sweep): every warp arms its
+ *          first stage of rows for 16 bytes more, waits at most `limit` ns, lets its copies land
+ *          and stops; the run's status is APPFIS_GB_ETIMEOUT.
  *  kind 0: clears a pending plan. */
 APPFIS_GB_API int appfis_gb_test_stall_next(int kind, unsigned long long limit);
 
@@ -322,6 +325,11 @@ typedef struct {
  * fields, step counts and dt logs of the two forms are identical. */
 #define APPFIS_GB_FLOOD_TWO_PHASE 2
 #define APPFIS_GB_FLOOD_FUSED 4
+/* The FP32 fused full sweep (no SKIP_DRY) streams each strip's rows into shared memory by TMA
+ * (bulk tensor copies of 4-row stages, one stage ahead of the computation) when every domain's
+ * arrays are 16-byte aligned and its pitch is a multiple of 4; UNSTAGED makes it load the rows
+ * directly (the same fields). */
+#define APPFIS_GB_FLOOD_UNSTAGED 8
 
 #define APPFIS_GB_FLOOD_MAX_DOMAINS 64
 

@@ -130,3 +130,87 @@ def test_fused_and_two_phase_flags_exclusive(gb, torch_cuda):
     with pytest.raises(_lib.AppfisError):
         _lib.flood_job(doms, 10.0, 0.5, 1e-3, 0.035, 60.0, 60.0, 1.0, max_steps=5,
                        flags=_lib.FLOOD_FUSED | _lib.FLOOD_TWO_PHASE)
+
+
+def _device_batch(torch, doms, pitch_of, offset=0):
+    """FP32 device domains set up from (dem, h) pairs: one buffer of 8 fields per domain (h0 h1
+    qx0 qx1 qy0 qy1 dem n2), row pitch pitch_of(nx), each field starting `offset` floats into
+    its own slab (an offset that is not a multiple of 4 leaves the rows 4-byte aligned only)."""
+    import ctypes
+    bufs, descs = [], (_lib.FloodDomain * len(doms))()
+    for k, (dem, h) in enumerate(doms):
+        ny, nx = dem.shape
+        pitch = pitch_of(nx)
+        slab = pitch * (ny + 2) + 8
+        f = torch.zeros(8 * slab, dtype=torch.float32, device="cuda")
+        bufs.append(f)
+        d = descs[k]
+        d.nx, d.ny, d.pitch = nx, ny, pitch
+        ptr = [f[m * slab + offset:].data_ptr() for m in range(8)]
+        d.h[0], d.h[1], d.qx[0], d.qx[1], d.qy[0], d.qy[1] = ptr[:6]
+        d.dem, d.n2 = ptr[6], ptr[7]
+        gb_dem = torch.from_numpy(dem).cuda()
+        gb_h = torch.from_numpy(h).cuda()
+        _lib.call("appfis_gb_flood_setup", ctypes.byref(d), _lib.F32, gb_dem.data_ptr(), gb_h.data_ptr(), None, None, 0.035,
+                  None)
+        torch.cuda.synchronize()
+    return bufs, descs
+
+
+def _device_run(torch, doms, flags, pitch_of, offset=0, steps=120):
+    import ctypes
+    bufs, descs = _device_batch(torch, doms, pitch_of, offset)
+    prm = _lib.FloodParams(10.0, 0.5, 1e-3, 300.0, 60.0, 1.0, 0.0, steps)
+    prm.flags = flags
+    st = torch.zeros(len(doms), dtype=torch.int32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    dtlog = torch.zeros(len(doms) * steps, dtype=torch.float64, device="cuda")
+    _lib.call("appfis_gb_flood_run", descs, len(doms), _lib.F32, ctypes.byref(prm), dtlog.data_ptr(), st.data_ptr(), None,
+              status.data_ptr(), None)
+    torch.cuda.synchronize()
+    assert int(status.item()) == _lib.OK
+    n = st.cpu().numpy()
+    out = []
+    for k, (dem, _) in enumerate(doms):
+        ny, nx = dem.shape
+        pitch, slab = pitch_of(nx), pitch_of(nx) * (ny + 2) + 8
+        b = int(n[k]) & 1
+        f = bufs[k]
+        fields = [f[m * slab + offset:m * slab + offset + pitch * (ny + 2)].view(ny + 2, pitch)[1:ny + 1, 1:nx + 1].cpu().numpy()
+                  for m in (b, 2 + b, 4 + b)]
+        out.append(fields)
+    return n.tolist(), out, dtlog.cpu().numpy()
+
+
+def test_staged_rows_bit_identical_to_row_loads(gb, torch_cuda):
+    """The fused FP32 full sweep with its rows staged by TMA (rows 16-byte aligned: pitch a
+    multiple of 4) against the same pass loading rows directly (UNSTAGED) and against the
+    two-phase form: every field, step count and dt identical.  Widths on and off the 28-column
+    strip grid and under one strip, rows not a multiple of 32, domains one row high and shorter
+    than a stage."""
+    skip = 0
+    doms = [W.triton_domain(97, 130, 11), W.triton_domain(64, 61, 12), W.triton_domain(150, 40, 13), W.triton_domain(5, 3, 14),
+            W.triton_domain(33, 56, 15), W.triton_domain(40, 29, 16), W.triton_domain(1, 70, 17), W.triton_domain(2, 27, 18)]
+    p4 = lambda nx: (nx + 2 + 3) // 4 * 4
+    staged = _device_run(torch_cuda, doms, _lib.FLOOD_FUSED | skip, p4)
+    rows = _device_run(torch_cuda, doms, _lib.FLOOD_FUSED | _lib.FLOOD_UNSTAGED | skip, p4)
+    two = _device_run(torch_cuda, doms, _lib.FLOOD_TWO_PHASE | skip, p4)
+    assert staged[0] == rows[0] == two[0]
+    assert np.array_equal(staged[2], rows[2]) and np.array_equal(staged[2], two[2])
+    for k in range(len(doms)):
+        for m in range(3):
+            assert np.array_equal(staged[1][k][m], rows[1][k][m]), (k, m)
+            assert np.array_equal(staged[1][k][m], two[1][k][m]), (k, m)
+
+
+def test_unaligned_rows_take_row_loads(gb, torch_cuda):
+    """Rows that are not 16-byte aligned (odd pitch, fields 4 bytes off a 16-byte boundary) cannot
+    be staged: the fused pass loads them directly and gives the same fields as an aligned run."""
+    doms = [W.triton_domain(45, 61, 21), W.triton_domain(30, 33, 22)]
+    odd = _device_run(torch_cuda, doms, _lib.FLOOD_FUSED, lambda nx: (nx + 2) | 1, offset=1, steps=60)
+    al = _device_run(torch_cuda, doms, _lib.FLOOD_FUSED, lambda nx: (nx + 2 + 3) // 4 * 4, steps=60)
+    assert odd[0] == al[0]
+    assert np.array_equal(odd[2], al[2])
+    for k in range(len(doms)):
+        for m in range(3):
+            assert np.array_equal(odd[1][k][m], al[1][k][m]), (k, m)

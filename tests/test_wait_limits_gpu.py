@@ -6,7 +6,10 @@ APPFIS_GB_ETIMEOUT, and the next call on the same device computes the right answ
   at the first barrier and each barrier wait gives up after 4096 polls (~64 ns sleep each).
 * The TMA-staged radius-4 star: each CTA arms its first plane's mbarrier for 16 bytes more than
   the copy delivers and waits at most 1 ms; it then lets its copies land (10 ms per pending
-  plane) and leaves; appfis_gb_stream_sync reads the device status word."""
+  plane) and leaves; appfis_gb_stream_sync reads the device status word.
+* The flood model's TMA-staged rows (FP32 fused pass): every warp arms its first stage of rows
+  for 16 bytes more than its copies deliver and waits at most 1 ms; it lets its copies land
+  (10 ms per pending stage), records the timeout and stops; the run reports APPFIS_GB_ETIMEOUT."""
 import ctypes
 
 import numpy as np
@@ -30,6 +33,20 @@ def test_flood_grid_barrier_wait_runs_out_then_recovers(gb, torch_cuda, flags):
     # the plan is used up: the same run now completes and matches a clean run's fields
     a = _lib.flood_job(doms, *args, max_steps=30, dtype=_lib.F32, flags=flags)
     b = _lib.flood_job(doms, *args, max_steps=30, dtype=_lib.F32, flags=flags)
+    assert a["steps"] == b["steps"] == [30, 30]
+    for k in range(2):
+        assert np.array_equal(a["h"][k], b["h"][k])
+
+
+def test_flood_staged_row_wait_runs_out_then_recovers(gb, torch_cuda):
+    doms = [W.triton_domain(70, 50, 3), W.triton_domain(40, 64, 4)]
+    args = (10.0, 0.5, 1e-3, 0.035, 600.0, 600.0, 1.0)
+    gb.call("appfis_gb_test_stall_next", 2, 1000000)  # 1 ms per wait
+    with pytest.raises(_lib.AppfisError) as e:
+        _lib.flood_job(doms, *args, max_steps=30, dtype=_lib.F32, flags=_lib.FLOOD_FUSED)
+    assert e.value.status == _lib.ETIMEOUT, str(e.value)
+    a = _lib.flood_job(doms, *args, max_steps=30, dtype=_lib.F32, flags=_lib.FLOOD_FUSED)
+    b = _lib.flood_job(doms, *args, max_steps=30, dtype=_lib.F32, flags=_lib.FLOOD_FUSED | _lib.FLOOD_UNSTAGED)
     assert a["steps"] == b["steps"] == [30, 30]
     for k in range(2):
         assert np.array_equal(a["h"][k], b["h"][k])
