@@ -3,6 +3,7 @@ rounding sequence except for cbrt (CUDA's and glibc's may differ in the last bit
 and every dt agree with the oracle (the reference's own CPU path, golden fixtures) to 1e-9.  FP32 form:
 within its stated error of the FP64 oracle.  Batches of uneven domains: each domain equals its
 own single-domain run."""
+import ctypes
 import glob
 import os
 
@@ -136,7 +137,6 @@ def _device_batch(torch, doms, pitch_of, offset=0):
     """FP32 device domains set up from (dem, h) pairs: one buffer of 8 fields per domain (h0 h1
     qx0 qx1 qy0 qy1 dem n2), row pitch pitch_of(nx), each field starting `offset` floats into
     its own slab (an offset that is not a multiple of 4 leaves the rows 4-byte aligned only)."""
-    import ctypes
     bufs, descs = [], (_lib.FloodDomain * len(doms))()
     for k, (dem, h) in enumerate(doms):
         ny, nx = dem.shape
@@ -158,7 +158,6 @@ def _device_batch(torch, doms, pitch_of, offset=0):
 
 
 def _device_run(torch, doms, flags, pitch_of, offset=0, steps=120):
-    import ctypes
     bufs, descs = _device_batch(torch, doms, pitch_of, offset)
     prm = _lib.FloodParams(10.0, 0.5, 1e-3, 300.0, 60.0, 1.0, 0.0, steps)
     prm.flags = flags
