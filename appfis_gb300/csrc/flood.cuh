@@ -546,8 +546,10 @@ struct RowRing {
 // array pointers are then read from shared memory where they are used instead of occupying 16
 // registers for the whole strip (90.5 against 87.4 G cell-steps/s on the 32-domain batch).
 // STAGED: rows come from the warp's TMA ring (`ring`, domain d's maps in p.maps); otherwise
-// from global memory, the row after next loaded while a row is computed.
-template <class T, bool STAGED = false>
+// from global memory, the row after next loaded while a row is computed.  QUIET: rows whose
+// neighbourhood is exactly dry take the short path below (the full sweep; with dry strips left
+// out the strips that remain are seldom dry and the votes would only cost).
+template <class T, bool STAGED = false, bool QUIET = true>
 __device__ bool phase_bf(const Dom<T>& D, long long local, int b, T dt, const Params& p, unsigned long long* dt_next,
                          RowRing* ring = nullptr, int d = 0, Ctl* ctl = nullptr)
 {
@@ -634,6 +636,13 @@ __device__ bool phase_bf(const Dom<T>& D, long long local, int b, T dt, const Pa
     T h1 = zero, qx1 = zero, qy1 = zero, z1 = zero;  // row r-1: updated state, bed
     T mn = K<T>::big();
     bool dry = true;  // every cell this lane owns ends with h = qx = qy = 0
+    // Quiet rows: when the depth of every cell of rows r-1 .. r+1 across the warp is exactly 0
+    // (no Y face r|r-1 was wet, and rows r and r+1 are zero), no face of row r has water on
+    // either side, so every face returns without a contribution and the update with zero
+    // right-hand sides leaves the depth (+0 or -0) and sets both momenta to +0 (hextra > 0):
+    // the same bits without the face arithmetic.
+    const bool qok = QUIET && hextra > zero;
+    bool dcur = QUIET && __all_sync(0xffffffffu, zero_bits(cj.h));
     for (int r = ra; r <= rb; r++) {
         const bool rin = r >= 1 && r <= ny;
         Raw<T> rnn;
@@ -646,37 +655,54 @@ __device__ bool phase_bf(const Dom<T>& D, long long local, int b, T dt, const Pa
             n2v = upd && rin ? n2[(size_t)r * px + i] : zero;
         }
         const Cell<T> cn_ = cell_of(rn);
-        // X face i|i+1 of row r: rhs0 of cell i, rhs1 of cell i+1 (the next lane)
-        const Cell<T> right = shfl_cell(cj, 1, true);
-        T xr1[3] = {zero, zero, zero}, xr2[3] = {zero, zero, zero};
-        bool xwet = false;
-        if (xface && rin) xwet = face<T>(cj, right, one, zero, dx, dt, hextra, xr1, xr2);
-        T lr[3];
-        lr[0] = __shfl_up_sync(0xffffffffu, xr2[0], 1);
-        lr[1] = __shfl_up_sync(0xffffffffu, xr2[1], 1);
-        lr[2] = __shfl_up_sync(0xffffffffu, xr2[2], 1);
-        const bool lwet = __shfl_up_sync(0xffffffffu, (int)xwet, 1) != 0;
-        // Y face r+1|r: id1 = row r+1, id2 = row r (row r's rhs1 and row r+1's rhs0)
-        T yn1[3] = {zero, zero, zero}, yr2[3] = {zero, zero, zero};
+        const bool dnext = QUIET && __all_sync(0xffffffffu, zero_bits(cn_.h));
+        const bool quiet = qok && dcur && dnext && !__any_sync(0xffffffffu, ywet);
+        dcur = dnext;
+        T yn1[3] = {zero, zero, zero};
         bool ynwet = false;
-        if (upd && r >= 0 && r <= ny) ynwet = face<T>(cn_, cj, zero, one, dx, dt, hextra, yn1, yr2);
         T hn = cj.h, qxn = cj.qx, qyn = cj.qy;
-        if (upd && rin) {
-            T r0[3], r1[3];
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                r0[k] = xwet ? xr1[k] : zero;
-                if (ywet) r0[k] = r0[k] + ycar[k];
-                r1[k] = lwet ? lr[k] : zero;
-                if (ynwet) r1[k] = r1[k] + yr2[k];
+        if (quiet) {
+            if (upd && rin) {
+                qxn = zero;
+                qyn = zero;
             }
-            update<T>(cj.h, cj.qx, cj.qy, n2v, r0, r1, dt, hextra, hn, qxn, qyn);
+        } else {
+            // X face i|i+1 of row r: rhs0 of cell i, rhs1 of cell i+1 (the next lane)
+            const Cell<T> right = shfl_cell(cj, 1, true);
+            T xr1[3] = {zero, zero, zero}, xr2[3] = {zero, zero, zero};
+            bool xwet = false;
+            if (xface && rin) xwet = face<T>(cj, right, one, zero, dx, dt, hextra, xr1, xr2);
+            T lr[3];
+            lr[0] = __shfl_up_sync(0xffffffffu, xr2[0], 1);
+            lr[1] = __shfl_up_sync(0xffffffffu, xr2[1], 1);
+            lr[2] = __shfl_up_sync(0xffffffffu, xr2[2], 1);
+            const bool lwet = __shfl_up_sync(0xffffffffu, (int)xwet, 1) != 0;
+            // Y face r+1|r: id1 = row r+1, id2 = row r (row r's rhs1 and row r+1's rhs0)
+            T yr2[3] = {zero, zero, zero};
+            if (upd && r >= 0 && r <= ny) ynwet = face<T>(cn_, cj, zero, one, dx, dt, hextra, yn1, yr2);
+            if (upd && rin) {
+                T r0[3], r1[3];
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    r0[k] = xwet ? xr1[k] : zero;
+                    if (ywet) r0[k] = r0[k] + ycar[k];
+                    r1[k] = lwet ? lr[k] : zero;
+                    if (ynwet) r1[k] = r1[k] + yr2[k];
+                }
+                update<T>(cj.h, cj.qx, cj.qy, n2v, r0, r1, dt, hextra, hn, qxn, qyn);
+            }
         }
         // row r-1, one of the strip's own rows: wet/dry fix (triton_appfis.hpp:1095-1112) on the
-        // updated state, then its CFL dt (:567-586), then the write
+        // updated state, then its CFL dt (:567-586), then the write; the neighbours' depth and
+        // bed are fetched only when some owned cell is wet enough to need them
         if (r - 1 >= j0 && r - 1 < j1) {
-            const T hL = __shfl_up_sync(0xffffffffu, h1, 1), hR = __shfl_down_sync(0xffffffffu, h1, 1);
-            const T zL = __shfl_up_sync(0xffffffffu, z1, 1), zR = __shfl_down_sync(0xffffffffu, z1, 1);
+            T hL = zero, hR = zero, zL = zero, zR = zero;
+            if (!QUIET || __any_sync(0xffffffffu, own && h1 > hextra)) {
+                hL = __shfl_up_sync(0xffffffffu, h1, 1);
+                hR = __shfl_down_sync(0xffffffffu, h1, 1);
+                zL = __shfl_up_sync(0xffffffffu, z1, 1);
+                zR = __shfl_down_sync(0xffffffffu, z1, 1);
+            }
             if (own) {
                 T qxr = qx1, qyr = qy1;
                 if (h1 > hextra) {
@@ -808,8 +834,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? FLOOD_F32_MIN_BLOCKS : 1
                     if (lane == 0) zout[s] = z;
                     return;
                 }
-                const bool dry = phase_bf<T, STAGED>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p, &ctl->dtbits[dn][d],
-                                                     &ring, d, ctl);
+                const bool dry = phase_bf<T, STAGED, false>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p,
+                                                            &ctl->dtbits[dn][d], &ring, d, ctl);
                 if (lane == 0) zout[s] = dry ? (unsigned char)(z < 2 ? z + 1 : 2) : 0;
             } else if (f & 4) {
                 phase_bf<T, STAGED>(doms[d], s - doms[d].strip0, f & 1, dc.dt[d], p, &ctl->dtbits[dn][d], &ring, d, ctl);

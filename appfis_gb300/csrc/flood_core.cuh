@@ -55,6 +55,17 @@ template <> struct K<float> {
     static __device__ __forceinline__ float dry() { return 1e-6f; }
 };
 
+// Exactly +0 or -0, tested on the bits (a float denormal, which the arithmetic flushes to zero,
+// does not count).
+template <class T>
+__device__ __forceinline__ bool zero_bits(T v)
+{
+    if constexpr (sizeof(T) == 4)
+        return (__float_as_uint(v) << 1) == 0u;
+    else
+        return ((unsigned long long)__double_as_longlong(v) << 1) == 0ull;
+}
+
 // A cell's state as the flux needs it.
 template <class T>
 struct Cell {

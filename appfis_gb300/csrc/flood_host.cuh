@@ -219,7 +219,7 @@ int run(const appfis_gb_flood_domain* doms, int ndom, const appfis_gb_flood_para
     p.tx_extra = 0;
     GB_TRY(upload_sources(doms, srcs, ndom, &p.srcs, st));
     // the fused FP32 full sweep stages its rows by TMA when every domain's arrays and rows are
-    // 16-byte aligned: 107.6 against 92.6 G cell-steps/s on the 32-domain batch.  With dry strips
+    // 16-byte aligned: 112.5 against 97.4 G cell-steps/s on the 32-domain batch.  With dry strips
     // left out it loads them directly (324 against 319: a warp's strips are then scattered, and
     // each one starts its ring from empty); so does UNSTAGED, or any other layout (same fields).
     bool staged = fused && std::is_same<T, float>::value && !(prm->flags & APPFIS_GB_FLOOD_UNSTAGED) &&
